@@ -1,0 +1,509 @@
+"""bonxai_gb300 -- GB300-native sparse voxel grid and probabilistic occupancy map.
+
+Python front end of the C ABI in include/bonxai_gb300.h (the C++ drop-in
+headers in include/bonxai/ and include/bonxai_map/ are the other front end).
+The classes mirror the reference's interface (bonxai_core/include/bonxai/
+bonxai.hpp: VoxelGrid; bonxai_map/include/bonxai_map/probabilistic_map.hpp:
+ProbabilisticMap) as batch calls: arrays of coordinates or points in, arrays
+out. Arrays may be numpy arrays (host) or CUDA torch tensors (device); the
+library stages host arrays itself.
+
+There is no CPU fallback: if the CUDA library is missing or no GPU is visible,
+constructing a map raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+__all__ = ["VoxelGrid", "ProbabilisticMap", "BonxaiError", "Config", "load_library",
+           "compute_rays", "library_path", "CLEAR_MEMORY", "SET_ALL_CELLS_OFF"]
+
+PKG = Path(__file__).resolve().parent
+_LIB_PATH = PKG / "_build" / "libbonxai_gb300.so"
+
+CLEAR_MEMORY = 0
+SET_ALL_CELLS_OFF = 1
+
+FLAG_KEEP_NONFINITE = 1
+FLAG_TIMING = 2
+
+STATUS = {0: "ok", 1: "invalid argument", 2: "node pool exhausted", 3: "root hash full",
+          4: "device wait timed out", 5: "CUDA error", 6: "no CUDA device",
+          7: "output buffer too small"}
+
+
+class BonxaiError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+class Config(C.Structure):
+    _fields_ = [("pool_budget_bytes", C.c_size_t), ("initial_leaves", C.c_uint32),
+                ("initial_inners", C.c_uint32), ("hash_buckets", C.c_uint32),
+                ("hash_load_factor", C.c_float), ("device", C.c_int),
+                ("stream", C.c_void_p), ("rays_per_warp", C.c_uint32),
+                ("block_size", C.c_uint32), ("flags", C.c_uint32)]
+
+    def __init__(self, **kw):
+        super().__init__()
+        self.device = -1
+        for k, v in kw.items():
+            setattr(self, k, v)
+
+
+class Options(C.Structure):
+    _fields_ = [("prob_miss_log", C.c_int32), ("prob_hit_log", C.c_int32),
+                ("clamp_min_log", C.c_int32), ("clamp_max_log", C.c_int32),
+                ("occupancy_threshold_log", C.c_int32)]
+
+
+_vp, _sz, _int, _dbl, _u64p = C.c_void_p, C.c_size_t, C.c_int, C.c_double, C.POINTER(C.c_uint64)
+_SIGS = {
+    "bxg_config_default": (None, [_vp]),
+    "bxg_status_string": (C.c_char_p, [_int]),
+    "bxg_version": (_int, []),
+    "bxg_last_error": (C.c_char_p, [_vp]),
+    "bxg_grid_create": (_int, [_vp, _dbl, _int, _int, _sz, _vp]),
+    "bxg_grid_destroy": (_int, [_vp]),
+    "bxg_grid_pos_to_coord": (_int, [_vp, _vp, _sz, _vp]),
+    "bxg_grid_set_values": (_int, [_vp, _vp, _vp, _sz, _vp]),
+    "bxg_grid_set_values_at_points_f32": (_int, [_vp, _vp, _sz, _sz, _vp]),
+    "bxg_grid_set_values_at_points_f64": (_int, [_vp, _vp, _sz, _sz, _vp]),
+    "bxg_grid_get_values": (_int, [_vp, _vp, _sz, _vp, _vp, _int]),
+    "bxg_grid_set_cells_on": (_int, [_vp, _vp, _sz, _vp, _vp]),
+    "bxg_grid_set_cells_off": (_int, [_vp, _vp, _sz, _vp]),
+    "bxg_grid_is_cell_on": (_int, [_vp, _vp, _sz, _vp]),
+    "bxg_grid_active_cells": (_int, [_vp, _vp]),
+    "bxg_grid_node_counts": (_int, [_vp, _vp, _vp]),
+    "bxg_grid_mem_usage": (_int, [_vp, _vp]),
+    "bxg_grid_dump": (_int, [_vp, _vp, _vp, _sz, _vp]),
+    "bxg_grid_clear": (_int, [_vp, _int]),
+    "bxg_grid_release_unused": (_int, [_vp]),
+    "bxg_grid_synchronize": (_int, [_vp]),
+    "bxg_pmap_create": (_int, [_vp, _dbl, _vp]),
+    "bxg_pmap_destroy": (_int, [_vp]),
+    "bxg_pmap_get_options": (_int, [_vp, _vp]),
+    "bxg_pmap_set_options": (_int, [_vp, _vp]),
+    "bxg_pmap_insert_point_cloud_f32": (_int, [_vp, _vp, _sz, _sz, _vp, _dbl, _vp]),
+    "bxg_pmap_insert_point_cloud_f64": (_int, [_vp, _vp, _sz, _sz, _vp, _dbl, _vp]),
+    "bxg_pmap_insert_point_cloud_f32_async": (_int, [_vp, _vp, _sz, _sz, _vp, _dbl]),
+    "bxg_pmap_add_hit_points": (_int, [_vp, _vp, _sz]),
+    "bxg_pmap_add_miss_points": (_int, [_vp, _vp, _sz]),
+    "bxg_pmap_update_free_cells": (_int, [_vp, _vp, _vp]),
+    "bxg_pmap_is_occupied": (_int, [_vp, _vp, _sz, _vp]),
+    "bxg_pmap_is_unknown": (_int, [_vp, _vp, _sz, _vp]),
+    "bxg_pmap_is_free": (_int, [_vp, _vp, _sz, _vp]),
+    "bxg_pmap_get_occupied": (_int, [_vp, _vp, _sz, _vp]),
+    "bxg_pmap_get_free": (_int, [_vp, _vp, _sz, _vp]),
+    "bxg_pmap_dump": (_int, [_vp, _vp, _vp, _sz, _vp]),
+    "bxg_pmap_active_cells": (_int, [_vp, _vp]),
+    "bxg_pmap_node_counts": (_int, [_vp, _vp, _vp]),
+    "bxg_pmap_mem_usage": (_int, [_vp, _vp]),
+    "bxg_pmap_update_count": (_int, [_vp, _vp]),
+    "bxg_pmap_clear": (_int, [_vp]),
+    "bxg_pmap_synchronize": (_int, [_vp]),
+    "bxg_pmap_last_stats": (_int, [_vp, _vp]),
+    "bxg_pmap_kernel_times": (_int, [_vp, _vp]),
+    "bxg_pmap_stream": (_vp, [_vp]),
+    "bxg_compute_rays": (_int, [_vp, _vp, _sz, _vp, _vp, _vp]),
+}
+
+_lib = None
+
+
+def library_path() -> Path:
+    return Path(os.environ.get("BONXAI_GB300_LIB", str(_LIB_PATH)))
+
+
+def load_library() -> C.CDLL:
+    """Loads the CUDA library; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        path = library_path()
+        if not path.exists():
+            raise ImportError(f"{path} is missing: run `python -m bonxai_gb300.build` "
+                              "(or __graft_entry__.build()) first; there is no CPU fallback")
+        lib = C.CDLL(str(path))
+        for name, (res, args) in _SIGS.items():
+            f = getattr(lib, name)
+            f.restype, f.argtypes = res, args
+        _lib = lib
+    return _lib
+
+
+# ----------------------------------------------------------------------------
+# array plumbing: numpy (host) or torch CUDA tensors (device)
+# ----------------------------------------------------------------------------
+def _is_torch(a) -> bool:
+    return type(a).__module__.startswith("torch")
+
+
+def _in(a, dtype, cols=None):
+    """(pointer, keepalive, n_rows) for an input array."""
+    if _is_torch(a):
+        import torch
+        tdt = {np.float32: torch.float32, np.float64: torch.float64, np.int32: torch.int32,
+               np.uint8: torch.uint8, np.uint32: torch.int32, np.int64: torch.int64}[dtype]
+        t = a.contiguous()
+        if t.dtype != tdt:
+            raise TypeError(f"expected {tdt}, got {t.dtype}")
+        n = t.shape[0] if t.dim() else 1
+        return C.c_void_p(t.data_ptr()), t, n
+    arr = np.ascontiguousarray(a, dtype=dtype)
+    if cols:
+        arr = arr.reshape(-1, cols)
+    return arr.ctypes.data_as(_vp), arr, (arr.shape[0] if arr.ndim else 1)
+
+
+def _ptr(arr):
+    if arr is None:
+        return None
+    if _is_torch(arr):
+        return C.c_void_p(arr.data_ptr())
+    return arr.ctypes.data_as(_vp)
+
+
+class _Handle:
+    _destroy = None
+
+    def _check(self, st: int):
+        if st != 0:
+            msg = self.lib.bxg_last_error(self.h)
+            raise BonxaiError(st, msg.decode() if msg else "")
+
+    def close(self):
+        if getattr(self, "h", None):
+            getattr(self.lib, self._destroy)(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+_VALUE_BYTES = {np.dtype(np.float32): 4, np.dtype(np.int32): 4, np.dtype(np.uint32): 4,
+                np.dtype(np.float64): 8, np.dtype(np.int64): 8, np.dtype(np.uint64): 8,
+                np.dtype(np.int16): 2, np.dtype(np.uint16): 2, np.dtype(np.int8): 1,
+                np.dtype(np.uint8): 1}
+
+
+class VoxelGrid(_Handle):
+    """VoxelGrid<T> (bonxai.hpp:114-333); dtype=None gives BinaryVoxelGrid."""
+    _destroy = "bxg_grid_destroy"
+
+    def __init__(self, voxel_size: float, inner_bits: int = 2, leaf_bits: int = 3,
+                 dtype=np.float32, config: Config | None = None):
+        self.lib = load_library()
+        self.dtype = None if dtype is None else np.dtype(dtype)
+        esz = 0 if dtype is None else _VALUE_BYTES[self.dtype]
+        h = C.c_void_p()
+        st = self.lib.bxg_grid_create(C.byref(h), float(voxel_size), int(inner_bits),
+                                      int(leaf_bits), esz, C.byref(config) if config else None)
+        if st:
+            raise BonxaiError(st, (self.lib.bxg_last_error(None) or b"").decode())
+        self.h = h
+        self.voxel_size = float(voxel_size)
+
+    def pos_to_coord(self, xyz):
+        p, keep, n = _in(xyz, np.float64, 3)
+        out = np.zeros((n, 3), np.int32)
+        self._check(self.lib.bxg_grid_pos_to_coord(self.h, p, n, _ptr(out)))
+        return out
+
+    posToCoord = pos_to_coord
+
+    def coord_to_pos(self, coords):
+        """coordToPos (bonxai.hpp:412-417): the cell corner coord * voxel_size."""
+        return np.asarray(coords, np.float64) * self.voxel_size
+
+    def set_values(self, coords, values, return_was_on: bool = False):
+        p, keep, n = _in(coords, np.int32, 3)
+        v, keepv, _ = (None, None, 0) if self.dtype is None else _in(values, self.dtype)
+        was = np.zeros(n, np.uint8) if return_was_on else None
+        self._check(self.lib.bxg_grid_set_values(self.h, p, v, n, _ptr(was)))
+        return was
+
+    setValue = set_values
+
+    def set_values_at_points(self, points, values):
+        dt = np.float64 if (getattr(points, "dtype", None) == np.float64 or
+                            str(getattr(points, "dtype", "")) == "torch.float64") else np.float32
+        p, keep, n = _in(points, dt, 3)
+        v, keepv, _ = (None, None, 0) if self.dtype is None else _in(values, self.dtype)
+        f = (self.lib.bxg_grid_set_values_at_points_f64 if dt == np.float64 else
+             self.lib.bxg_grid_set_values_at_points_f32)
+        self._check(f(self.h, p, 0, n, v))
+
+    def get_values(self, coords, create: bool = False):
+        p, keep, n = _in(coords, np.int32, 3)
+        vals = None if self.dtype is None else np.zeros(n, self.dtype)
+        found = np.zeros(n, np.uint8)
+        self._check(self.lib.bxg_grid_get_values(self.h, p, n, _ptr(vals), _ptr(found),
+                                                 int(create)))
+        return vals, found
+
+    value = get_values
+
+    def set_cells_on(self, coords, default=0):
+        p, keep, n = _in(coords, np.int32, 3)
+        d = None if self.dtype is None else np.array([default], self.dtype)
+        was = np.zeros(n, np.uint8)
+        self._check(self.lib.bxg_grid_set_cells_on(self.h, p, n, _ptr(d), _ptr(was)))
+        return was
+
+    def set_cells_off(self, coords):
+        p, keep, n = _in(coords, np.int32, 3)
+        was = np.zeros(n, np.uint8)
+        self._check(self.lib.bxg_grid_set_cells_off(self.h, p, n, _ptr(was)))
+        return was
+
+    def is_cell_on(self, coords):
+        p, keep, n = _in(coords, np.int32, 3)
+        out = np.zeros(n, np.uint8)
+        self._check(self.lib.bxg_grid_is_cell_on(self.h, p, n, _ptr(out)))
+        return out
+
+    def active_cells_count(self) -> int:
+        out = C.c_size_t()
+        self._check(self.lib.bxg_grid_active_cells(self.h, C.byref(out)))
+        return out.value
+
+    activeCellsCount = active_cells_count
+
+    def node_counts(self):
+        r, l = C.c_size_t(), C.c_size_t()
+        self._check(self.lib.bxg_grid_node_counts(self.h, C.byref(r), C.byref(l)))
+        return r.value, l.value
+
+    def mem_usage(self) -> int:
+        out = C.c_size_t()
+        self._check(self.lib.bxg_grid_mem_usage(self.h, C.byref(out)))
+        return out.value
+
+    def dump(self, sort: bool = True):
+        """forEachCell as arrays: (coords int32 [n,3], values [n]) sorted by xyz."""
+        n = self.active_cells_count()
+        xyz = np.zeros((max(n, 1), 3), np.int32)
+        vals = None if self.dtype is None else np.zeros(max(n, 1), self.dtype)
+        got = C.c_size_t()
+        self._check(self.lib.bxg_grid_dump(self.h, _ptr(xyz), _ptr(vals), n, C.byref(got)))
+        xyz = xyz[:got.value]
+        vals = None if vals is None else vals[:got.value]
+        if sort:
+            o = np.lexsort((xyz[:, 2], xyz[:, 1], xyz[:, 0]))
+            xyz = xyz[o]
+            vals = None if vals is None else vals[o]
+        return xyz, vals
+
+    def for_each_cell(self, func):
+        xyz, vals = self.dump(sort=False)
+        for k in range(len(xyz)):
+            func(None if vals is None else vals[k], tuple(int(c) for c in xyz[k]))
+
+    forEachCell = for_each_cell
+
+    def clear(self, option: int = CLEAR_MEMORY):
+        self._check(self.lib.bxg_grid_clear(self.h, int(option)))
+
+    def release_unused_memory(self):
+        self._check(self.lib.bxg_grid_release_unused(self.h))
+
+    releaseUnusedMemory = release_unused_memory
+
+
+class ProbabilisticMap(_Handle):
+    """ProbabilisticMap (probabilistic_map.hpp:27-137) on one GPU."""
+    _destroy = "bxg_pmap_destroy"
+
+    def __init__(self, resolution: float, config: Config | None = None):
+        self.lib = load_library()
+        h = C.c_void_p()
+        st = self.lib.bxg_pmap_create(C.byref(h), float(resolution),
+                                      C.byref(config) if config else None)
+        if st:
+            raise BonxaiError(st, (self.lib.bxg_last_error(None) or b"").decode())
+        self.h = h
+        self.resolution = float(resolution)
+
+    @property
+    def options(self) -> np.ndarray:
+        o = Options()
+        self._check(self.lib.bxg_pmap_get_options(self.h, C.byref(o)))
+        return np.array([o.prob_miss_log, o.prob_hit_log, o.clamp_min_log, o.clamp_max_log,
+                         o.occupancy_threshold_log], np.int32)
+
+    @options.setter
+    def options(self, v):
+        v = [int(x) for x in v]
+        o = Options(*v)
+        self._check(self.lib.bxg_pmap_set_options(self.h, C.byref(o)))
+
+    @property
+    def update_count(self) -> int:
+        out = C.c_int()
+        self._check(self.lib.bxg_pmap_update_count(self.h, C.byref(out)))
+        return out.value
+
+    @property
+    def stream(self) -> int:
+        return self.lib.bxg_pmap_stream(self.h) or 0
+
+    def insert_point_cloud(self, points, origin, max_range: float, stride: int = 0) -> int:
+        """insertPointCloud; returns V = points + cast ray cells."""
+        is64 = (getattr(points, "dtype", None) == np.float64 or
+                str(getattr(points, "dtype", "")) == "torch.float64")
+        dt = np.float64 if is64 else np.float32
+        p, keep, n = _in(points, dt, None if stride else 3)
+        o = np.ascontiguousarray(np.asarray(origin, dt).reshape(3))
+        v = C.c_uint64()
+        f = (self.lib.bxg_pmap_insert_point_cloud_f64 if is64 else
+             self.lib.bxg_pmap_insert_point_cloud_f32)
+        if stride:
+            n = n  # caller passes rows already
+        self._check(f(self.h, p, int(stride), n, _ptr(o), float(max_range), C.byref(v)))
+        return v.value
+
+    insertPointCloud = insert_point_cloud
+
+    def insert_point_cloud_async(self, points, origin, max_range: float):
+        p, keep, n = _in(points, np.float32, 3)
+        o = np.ascontiguousarray(np.asarray(origin, np.float32).reshape(3))
+        self._check(self.lib.bxg_pmap_insert_point_cloud_f32_async(self.h, p, 0, n, _ptr(o),
+                                                                   float(max_range)))
+        self._keep = (keep, o)
+
+    def add_hit_points(self, points):
+        p, keep, n = _in(points, np.float64, 3)
+        self._check(self.lib.bxg_pmap_add_hit_points(self.h, p, n))
+
+    def add_miss_points(self, points):
+        p, keep, n = _in(points, np.float64, 3)
+        self._check(self.lib.bxg_pmap_add_miss_points(self.h, p, n))
+
+    addHitPoint = add_hit_points
+    addMissPoint = add_miss_points
+
+    def update_free_cells(self, origin) -> int:
+        o = np.ascontiguousarray(np.asarray(origin, np.float64).reshape(3))
+        v = C.c_uint64()
+        self._check(self.lib.bxg_pmap_update_free_cells(self.h, _ptr(o), C.byref(v)))
+        return v.value
+
+    updateFreeCells = update_free_cells
+
+    def _query(self, fn, coords, out=None):
+        p, keep, n = _in(coords, np.int32, 3)
+        if out is None:
+            out = np.zeros(n, np.uint8)
+        self._check(fn(self.h, p, n, _ptr(out)))
+        return out
+
+    def is_occupied(self, coords, out=None):
+        return self._query(self.lib.bxg_pmap_is_occupied, coords, out)
+
+    def is_unknown(self, coords, out=None):
+        return self._query(self.lib.bxg_pmap_is_unknown, coords, out)
+
+    def is_free(self, coords, out=None):
+        return self._query(self.lib.bxg_pmap_is_free, coords, out)
+
+    isOccupied, isUnknown, isFree = is_occupied, is_unknown, is_free
+
+    def active_cells_count(self) -> int:
+        out = C.c_size_t()
+        self._check(self.lib.bxg_pmap_active_cells(self.h, C.byref(out)))
+        return out.value
+
+    def node_counts(self):
+        r, l = C.c_size_t(), C.c_size_t()
+        self._check(self.lib.bxg_pmap_node_counts(self.h, C.byref(r), C.byref(l)))
+        return r.value, l.value
+
+    def mem_usage(self) -> int:
+        out = C.c_size_t()
+        self._check(self.lib.bxg_pmap_mem_usage(self.h, C.byref(out)))
+        return out.value
+
+    def _coords(self, fn, sort=True):
+        got = C.c_size_t()
+        st = fn(self.h, None, 0, C.byref(got))
+        if st not in (0, 7):
+            self._check(st)
+        n = got.value
+        out = np.zeros((max(n, 1), 3), np.int32)
+        self._check(fn(self.h, _ptr(out), n, C.byref(got)))
+        out = out[:got.value]
+        if sort:
+            out = out[np.lexsort((out[:, 2], out[:, 1], out[:, 0]))]
+        return out
+
+    def get_occupied_voxels(self, sort: bool = True):
+        return self._coords(self.lib.bxg_pmap_get_occupied, sort)
+
+    def get_free_voxels(self, sort: bool = True):
+        return self._coords(self.lib.bxg_pmap_get_free, sort)
+
+    getOccupiedVoxels, getFreeVoxels = get_occupied_voxels, get_free_voxels
+
+    def dump(self, sort: bool = True):
+        """Every cell as (coords [n,3] int32, packed CellT words [n] int32)."""
+        n = self.active_cells_count()
+        xyz = np.zeros((max(n, 1), 3), np.int32)
+        cells = np.zeros(max(n, 1), np.int32)
+        got = C.c_size_t()
+        self._check(self.lib.bxg_pmap_dump(self.h, _ptr(xyz), _ptr(cells), n, C.byref(got)))
+        xyz, cells = xyz[:got.value], cells[:got.value]
+        if sort:
+            o = np.lexsort((xyz[:, 2], xyz[:, 1], xyz[:, 0]))
+            xyz, cells = xyz[o], cells[o]
+        return xyz, cells
+
+    def clear(self):
+        self._check(self.lib.bxg_pmap_clear(self.h))
+
+    def synchronize(self):
+        self._check(self.lib.bxg_pmap_synchronize(self.h))
+
+    def last_stats(self) -> dict:
+        out = (C.c_uint64 * 8)()
+        self._check(self.lib.bxg_pmap_last_stats(self.h, out))
+        keys = ["points", "cast_rays", "ray_cells_visited", "ray_cells_updated", "leaves",
+                "launches"]
+        return {k: int(out[i]) for i, k in enumerate(keys)}
+
+    def kernel_times(self) -> list[float]:
+        out = (C.c_float * 4)()
+        self._check(self.lib.bxg_pmap_kernel_times(self.h, out))
+        return [float(x) for x in out]
+
+
+def compute_rays(origins, ends):
+    """ComputeRay for each (origin, end) pair on the GPU: list of [len,3] arrays."""
+    lib = load_library()
+    o, ko, n = _in(origins, np.int32, 3)
+    e, ke, _ = _in(ends, np.int32, 3)
+    lens = np.zeros(n, np.uint32)
+    st = lib.bxg_compute_rays(o, e, n, _ptr(lens), None, None)
+    if st:
+        raise BonxaiError(st, "compute_rays")
+    off = np.zeros(n, np.uint64)
+    off[1:] = np.cumsum(lens[:-1].astype(np.uint64))
+    total = int(lens.astype(np.uint64).sum())
+    cells = np.zeros((max(total, 1), 3), np.int32)
+    st = lib.bxg_compute_rays(o, e, n, _ptr(lens), _ptr(off), _ptr(cells))
+    if st:
+        raise BonxaiError(st, "compute_rays")
+    return [cells[int(off[i]):int(off[i]) + int(lens[i])] for i in range(n)]

@@ -1,0 +1,147 @@
+// Host-side state shared by the grid and probabilistic-map entry points.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstring>
+#include <string>
+
+#include "bonxai_gb300.h"
+#include "bxg_device.cuh"
+
+namespace bxg {
+
+// A growable device buffer.
+struct DevBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+  cudaError_t ensure(size_t bytes) {
+    if (bytes <= cap) return cudaSuccess;
+    size_t want = cap ? cap : 4096;
+    while (want < bytes) want *= 2;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    cudaError_t e = cudaMalloc(&p, want);
+    if (e == cudaSuccess) cap = want;
+    return e;
+  }
+  // Like ensure, but keeps the first `keep` bytes of the old content.
+  cudaError_t ensure_keep(size_t bytes, size_t keep, cudaStream_t s) {
+    if (bytes <= cap) return cudaSuccess;
+    size_t want = cap ? cap : 4096;
+    while (want < bytes) want *= 2;
+    void* np = nullptr;
+    cudaError_t e = cudaMalloc(&np, want);
+    if (e != cudaSuccess) return e;
+    if (p && keep) {
+      e = cudaMemcpyAsync(np, p, keep < cap ? keep : cap, cudaMemcpyDeviceToDevice, s);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+      if (e != cudaSuccess) {
+        cudaFree(np);
+        return e;
+      }
+    }
+    if (p) cudaFree(p);
+    p = np;
+    cap = want;
+    return cudaSuccess;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = default;
+  DevBuf& operator=(const DevBuf&) = default;
+  ~DevBuf() { release(); }
+  template <class T>
+  T* as() const {
+    return static_cast<T*>(p);
+  }
+};
+
+// One map: pools, counters, stream, scratch and error text.
+struct MapCore {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  uint32_t flags = 0;
+  double res = 0, inv_res = 0;
+  DMap dm{};
+  size_t budget = 0;
+  float load_factor = 0.5f;
+  uint32_t rays_per_warp = 0, block_size = 0;
+
+  // pools
+  DevBuf buckets, ichild, imask, lmask, ldata, lkey, lfree, ctr;
+  uint32_t* h_ctr = nullptr;  // pinned mirror of ctr
+
+  // scratch
+  DevBuf s_in, s_in2, s_out, s_out2, s_dedup, s_dedup2, s_ep, s_cast, s_tmp;
+
+  std::string err;
+  uint64_t launches = 0;
+  int sm_count = 0;
+
+  ~MapCore();
+};
+
+// Pointer kind.
+bool is_device_ptr(const void* p);
+
+int set_error(MapCore* m, int status, const std::string& msg);
+int cuda_fail(MapCore* m, cudaError_t e, const char* what);
+
+// Lifecycle and pools (bxg_core.cu).
+int core_init(MapCore* m, double res, int ib, int lb, size_t esz, const bxg_config* cfg);
+int core_clear(MapCore* m);
+// Reads the counters back (synchronising the stream) and converts device error
+// bits into a status; clears them and repairs overshooting allocation counters.
+int core_sync(MapCore* m, uint32_t* err_bits_out = nullptr);
+// Grows pools ahead of need (after a sync).
+int core_maintain(MapCore* m);
+// Grows what the error bits say ran out; returns BXG_OK if a retry may succeed.
+int core_grow_for(MapCore* m, uint32_t err_bits);
+size_t core_mem_usage(const MapCore* m);
+int core_dump(MapCore* m, int32_t* out_xyz, void* out_values, size_t cap, size_t* n_out,
+              int filter, int32_t thr);
+int core_active_cells(MapCore* m, size_t* out);
+int core_node_counts(MapCore* m, size_t* roots, size_t* leaves);
+
+// Staging of caller arrays that may live on the host.
+// Returns a device pointer holding `bytes` of `src` (copied if host memory).
+int stage_in(MapCore* m, DevBuf& buf, const void* src, size_t bytes, const void** dev);
+// Returns a device pointer to write `bytes` into; after the kernels call
+// stage_out_finish to copy it to `dst` when dst is host memory.
+int stage_out(MapCore* m, DevBuf& buf, void* dst, size_t bytes, void** dev);
+int stage_out_finish(MapCore* m, void* dst, const void* dev, size_t bytes);
+
+inline unsigned long long* stats_of(const MapCore* m) {
+  return reinterpret_cast<unsigned long long*>(m->ctr.as<uint32_t>() + C_STATS);
+}
+
+#define BXG_CUDA(m, call)                                  \
+  do {                                                     \
+    cudaError_t e_ = (call);                               \
+    if (e_ != cudaSuccess) return cuda_fail((m), e_, #call); \
+  } while (0)
+
+#define BXG_LAUNCHED(m)                                        \
+  do {                                                         \
+    (m)->launches++;                                           \
+    cudaError_t e_ = cudaGetLastError();                       \
+    if (e_ != cudaSuccess) return cuda_fail((m), e_, "launch"); \
+  } while (0)
+
+// Shared kernels (bxg_core.cu).
+void launch_dedup_clear(MapCore* m, uint4* tab, uint32_t cap);
+// Inserts the non-empty buckets of old_b[0..old_cap) into the table of M.
+void launch_rehash(MapCore* m, const uint4* old_b, uint32_t old_cap, const DMap& M);
+// Text of the last failed create call on this host thread.
+void set_create_error(const std::string& msg);
+const MapCore* core_of_handle(const void* handle);
+
+}  // namespace bxg

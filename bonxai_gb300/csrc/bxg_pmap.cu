@@ -1,0 +1,880 @@
+// ProbabilisticMap on the GPU: insertPointCloud / addHitPoint / addMissPoint /
+// updateFreeCells / isOccupied / getOccupiedVoxels, bit-exact with
+// bonxai_map/include/bonxai_map/probabilistic_map.hpp and
+// bonxai_map/src/probabilistic_map.cpp.
+//
+// Why a scan parallelises without changing its result. Let u be the scan
+// counter (1, 2, 3, cycling; probabilistic_map.cpp:103-105).
+//  * Endpoint phase (insertPointCloud loop + addHit/MissPoint, hpp:146-158,
+//    cpp:30-54). Only endpoint cells change, and each changes at most once:
+//    the first point (lowest input index) that lands in a cell whose
+//    update_id != u updates it and queues one ray; every later point in that
+//    cell sees update_id == u and does nothing. A cell that already had
+//    update_id == u before the scan is neither updated nor ray-cast. So the
+//    outcome per cell depends only on its pre-scan word and the lowest index
+//    landing in it.
+//  * Ray phase (updateFreeCells, cpp:77-106). Every queued ray visits the
+//    origin cell and the next max-1 Bresenham cells; each visited cell is
+//    created (T{} = {0, 0}) and, if its update_id != u, becomes
+//    {max(p + miss, clamp_min), u}. After the endpoint phase the only writes
+//    are this one function of the word, so the order of rays and cells is
+//    irrelevant and racing writers store the same value: a plain load and a
+//    conditional store suffice.
+//
+// Kernels per scan (all on the handle's stream):
+//   k_endpoints   fp64 endpoint of each point, exactly as hpp:147-156 rounds
+//                 it; lowest index per endpoint cell via a scratch hash table.
+//   k_winners     the lowest-index point of each cell reads the pre-scan word;
+//                 unless update_id == u it appends {cell, hit/miss} to the ray
+//                 list (and counts the ray length for the ray-cell total).
+//   k_apply       each listed endpoint creates its cell and applies hit/miss.
+//   k_rays        lane-strided Bresenham over every listed ray: a group of W
+//                 lanes walks one ray, W consecutive cells per step, creating
+//                 leaves on the way and applying the miss update.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "bxg_internal.h"
+
+struct bxg_pmap_s {
+  bxg::MapCore core;
+  bxg_pmap_options opt{};
+  int update_count = 1;           // _update_count (probabilistic_map.hpp:129)
+  uint64_t cast_ub = 0;           // upper bound of queued rays on the device
+  uint64_t last_stats[8] = {0};
+  float last_times[4] = {0};
+  cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  ~bxg_pmap_s() {
+    for (auto& e : ev)
+      if (e) cudaEventDestroy(e);
+  }
+};
+
+namespace bxg {
+
+struct Opts {
+  int32_t miss, hit, cmin, cmax;
+};
+
+// ---------------------------------------------------------------------------
+// endpoint phase
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ bool finite3(double a, double b, double c) {
+  return isfinite(a) && isfinite(b) && isfinite(c);
+}
+
+// Lowest index per endpoint cell (scratch table, all-ones = empty).
+__device__ __forceinline__ void dedup_min_insert(uint4* tab, uint32_t tmask, int x, int y, int z,
+                                                 uint32_t i, const DMap& M) {
+  const uint4 kEmpty = make_uint4(kNone, kNone, kNone, kNone);
+  const uint4 mine = make_uint4(uint32_t(x), uint32_t(y), uint32_t(z), i);
+  uint32_t h = cell_hash(x, y, z) & tmask;
+  for (uint32_t p = 0; p <= tmask; ++p, h = (h + 1) & tmask) {
+    const uint4 old = cas128(tab + h, kEmpty, mine);
+    if (eq4(old, kEmpty)) return;
+    if (key_eq(old, x, y, z)) {
+      atomicMin(&tab[h].w, i);
+      return;
+    }
+  }
+  set_err(M, ERR_SCRATCH);
+}
+
+__device__ __forceinline__ uint32_t dedup_lookup(const uint4* tab, uint32_t tmask, int x, int y,
+                                                 int z) {
+  uint32_t h = cell_hash(x, y, z) & tmask;
+  for (uint32_t p = 0; p <= tmask; ++p, h = (h + 1) & tmask) {
+    const uint4 b = tab[h];
+    if (b.w == kNone) return kNone;
+    if (key_eq(b, x, y, z)) return b.w;
+  }
+  return kNone;
+}
+
+// insertPointCloud's per-point math (probabilistic_map.hpp:144-156) in double
+// with one IEEE rounding per operation and no contraction:
+//   v = to - from; sq = (vx*vx + vy*vy) + vz*vz;
+//   sq >= max_range^2 ? miss at from + (v / sqrt(sq)) * max_range : hit at to
+// then posToCoord = floor(p * inv_resolution) (bonxai.hpp:404-410).
+template <typename PT>
+__global__ void k_endpoints(DMap M, const uint8_t* __restrict__ pts, size_t stride, uint32_t n,
+                            double fx, double fy, double fz, double max_range, double mr2,
+                            double inv_res, int keep_nonfinite, int4* __restrict__ ep,
+                            uint4* tab, uint32_t tmask) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const PT* p = reinterpret_cast<const PT*>(pts + size_t(i) * stride);
+  const double tx = static_cast<double>(p[0]), ty = static_cast<double>(p[1]),
+               tz = static_cast<double>(p[2]);
+  if (!keep_nonfinite && !finite3(tx, ty, tz)) {
+    ep[i] = make_int4(0, 0, 0, EP_SKIP);
+    return;
+  }
+  const double vx = __dsub_rn(tx, fx), vy = __dsub_rn(ty, fy), vz = __dsub_rn(tz, fz);
+  const double sq = __dadd_rn(__dadd_rn(__dmul_rn(vx, vx), __dmul_rn(vy, vy)), __dmul_rn(vz, vz));
+  double ex, ey, ez;
+  int kind;
+  if (sq >= mr2) {
+    const double s = __dsqrt_rn(sq);
+    ex = __dadd_rn(fx, __dmul_rn(__ddiv_rn(vx, s), max_range));
+    ey = __dadd_rn(fy, __dmul_rn(__ddiv_rn(vy, s), max_range));
+    ez = __dadd_rn(fz, __dmul_rn(__ddiv_rn(vz, s), max_range));
+    kind = EP_MISS;
+  } else {
+    ex = tx;
+    ey = ty;
+    ez = tz;
+    kind = EP_HIT;
+  }
+  const int cx = __double2int_rd(__dmul_rn(ex, inv_res));
+  const int cy = __double2int_rd(__dmul_rn(ey, inv_res));
+  const int cz = __double2int_rd(__dmul_rn(ez, inv_res));
+  ep[i] = make_int4(cx, cy, cz, kind);
+  dedup_min_insert(tab, tmask, cx, cy, cz, i, M);
+}
+
+// addHitPoint / addMissPoint batches: double points with a given kind.
+__global__ void k_endpoints_kind(DMap M, const double* __restrict__ pts, uint32_t n, int kind,
+                                 double inv_res, int4* __restrict__ ep, uint4* tab,
+                                 uint32_t tmask) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int cx = __double2int_rd(__dmul_rn(pts[3 * i + 0], inv_res));
+  const int cy = __double2int_rd(__dmul_rn(pts[3 * i + 1], inv_res));
+  const int cz = __double2int_rd(__dmul_rn(pts[3 * i + 2], inv_res));
+  ep[i] = make_int4(cx, cy, cz, kind);
+  dedup_min_insert(tab, tmask, cx, cy, cz, i, M);
+}
+
+__device__ __forceinline__ uint32_t chebyshev(int ox, int oy, int oz, int x, int y, int z) {
+  const uint32_t dx = static_cast<uint32_t>(abs(x - ox)), dy = static_cast<uint32_t>(abs(y - oy)),
+                 dz = static_cast<uint32_t>(abs(z - oz));
+  return max(dx, max(dy, dz));
+}
+
+// The lowest-index point of each endpoint cell decides: no update and no ray
+// if the cell exists with update_id == u, else it joins the ray list.
+__global__ void k_winners(DMap M, const int4* __restrict__ ep, uint32_t n,
+                          const uint4* __restrict__ tab, uint32_t tmask, int ox, int oy, int oz,
+                          int32_t u, int4* __restrict__ cast, uint32_t cast_cap) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  bool add = false;
+  int4 e = make_int4(0, 0, 0, EP_SKIP);
+  if (i < n) {
+    e = ep[i];
+    if (e.w != EP_SKIP && dedup_lookup(tab, tmask, e.x, e.y, e.z) == i) {
+      add = true;
+      const uint32_t lf = leaf_of(M, e.x, e.y, e.z, false);
+      if (lf != kNone) {
+        const uint32_t ci = leaf_index(M, e.x, e.y, e.z);
+        if (cell_is_on(M, lf, ci)) {
+          const int32_t w = reinterpret_cast<const int32_t*>(M.ldata)[size_t(lf) * M.lsize + ci];
+          if (cell_id(w) == u) add = false;
+        }
+      }
+    }
+  }
+  const unsigned lane = threadIdx.x & 31;
+  const unsigned valid = __ballot_sync(0xffffffffu, i < n && e.w != EP_SKIP);
+  const unsigned am = __ballot_sync(0xffffffffu, add);
+  unsigned long long len = add ? chebyshev(ox, oy, oz, e.x, e.y, e.z) : 0;
+  len = __reduce_add_sync(0xffffffffu, static_cast<unsigned>(len));
+  uint32_t base = 0;
+  if (lane == 0) {
+    unsigned long long* st = reinterpret_cast<unsigned long long*>(M.ctr + C_STATS);
+    if (valid) atomicAdd(st + S_POINTS, static_cast<unsigned long long>(__popc(valid)));
+    if (len) atomicAdd(st + S_RAY_LEN, len);
+    if (am) base = atomicAdd(M.ctr + C_CAST, static_cast<uint32_t>(__popc(am)));
+  }
+  base = __shfl_sync(0xffffffffu, base, 0);
+  if (add) {
+    const uint32_t k = base + __popc(am & ((1u << lane) - 1));
+    if (k < cast_cap)
+      cast[k] = e;
+    else
+      set_err(M, ERR_SCRATCH);
+  }
+}
+
+// Creates each listed endpoint cell and applies its hit or miss
+// (probabilistic_map.cpp:35-41,49-54). Idempotent: a cell already at u is
+// left alone, so a retry after pool growth is safe.
+__global__ void k_apply(DMap M, const int4* __restrict__ cast, uint32_t cast_cap, int32_t u,
+                        Opts o) {
+  const uint32_t n = min(ld_volatile(M.ctr + C_CAST), cast_cap);
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const int4 e = cast[k];
+    const uint32_t lf = leaf_of(M, e.x, e.y, e.z, true);
+    if (lf == kNone) continue;
+    const uint32_t ci = leaf_index(M, e.x, e.y, e.z);
+    cell_mark_on(M, lf, ci);
+    int32_t* cp = reinterpret_cast<int32_t*>(M.ldata) + size_t(lf) * M.lsize + ci;
+    const int32_t w = *cp;
+    if (cell_id(w) != u) {
+      const int32_t p = cell_prob(w);
+      const int32_t np = e.w == EP_HIT ? min(wrap_add(p, o.hit), o.cmax)
+                                       : max(wrap_add(p, o.miss), o.cmin);
+      *cp = cell_pack(np, u);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// ray phase
+// ---------------------------------------------------------------------------
+// One group of W lanes walks one ray; lane sl handles k = sl, sl+W, ...
+// Consecutive lanes hold consecutive cells, so the lanes of one step touch a
+// few leaves: the first lane of each leaf run (a "head") looks the leaf up or
+// creates it, and the others take its slot by shuffle. The group keeps the
+// last leaf and root between steps.
+template <int W>
+__global__ void __launch_bounds__(256) k_rays(DMap M, const int4* __restrict__ cast,
+                                              uint32_t cast_cap, int ox, int oy, int oz,
+                                              int32_t u, int32_t miss, int32_t cmin) {
+  const uint32_t n_cast = min(ld_volatile(M.ctr + C_CAST), cast_cap);
+  const unsigned lane = threadIdx.x & 31;
+  const unsigned sl = lane & (W - 1);
+  const unsigned gbase = lane & ~(W - 1);
+  const unsigned gmask = (W == 32) ? 0xffffffffu : (((1u << W) - 1u) << gbase);
+  const uint32_t gid = (blockIdx.x * blockDim.x + threadIdx.x) / W;
+  const uint32_t ngroups = (gridDim.x * blockDim.x) / W;
+  const int32_t lm = leaf_mask(M);
+  const int32_t rm = root_mask(M);
+  uint32_t visited = 0, updated = 0;
+
+  for (uint32_t r = gid; r < n_cast; r += ngroups) {
+    const int4 e = cast[r];
+    const int dx = e.x - ox, dy = e.y - oy, dz = e.z - oz;
+    const uint32_t ax = static_cast<uint32_t>(abs(dx)), ay = static_cast<uint32_t>(abs(dy)),
+                   az = static_cast<uint32_t>(abs(dz));
+    const uint32_t m = max(ax, max(ay, az));
+    if (m == 0) continue;  // origin == end: no ray (probabilistic_map.hpp:164-166)
+    if (m >= kMaxRayCells) {
+      if (sl == 0) set_err(M, ERR_RAY_TOO_LONG);
+      continue;
+    }
+    const int sx = dx < 0 ? -1 : 1, sy = dy < 0 ? -1 : 1, sz = dz < 0 ? -1 : 1;
+    const uint32_t two_m = 2u * m;
+    const float rtm = __frcp_rn(static_cast<float>(two_m));
+    AxisStep X, Y, Z;
+    axis_init(X, ax, m, two_m, rtm, sl, W);
+    axis_init(Y, ay, m, two_m, rtm, sl, W);
+    axis_init(Z, az, m, two_m, rtm, sl, W);
+    int pkx = kEmptyKey, pky = kEmptyKey, pkz = kEmptyKey;  // group's last leaf key
+    uint32_t pleaf = kNone;
+    int rkx = kEmptyKey, rky = kEmptyKey, rkz = kEmptyKey;  // group's last root
+    uint32_t rin = kNone;
+
+    for (uint32_t base = 0; base < m; base += W) {
+      const bool act = base + sl < m;
+      const int cx = ox + sx * static_cast<int>(X.n);
+      const int cy = oy + sy * static_cast<int>(Y.n);
+      const int cz = oz + sz * static_cast<int>(Z.n);
+      const int lkx = cx & lm, lky = cy & lm, lkz = cz & lm;
+      int qx = __shfl_up_sync(gmask, lkx, 1, W);
+      int qy = __shfl_up_sync(gmask, lky, 1, W);
+      int qz = __shfl_up_sync(gmask, lkz, 1, W);
+      if (sl == 0) {
+        qx = pkx;
+        qy = pky;
+        qz = pkz;
+      }
+      const bool head = act && (lkx != qx || lky != qy || lkz != qz);
+      uint32_t leaf = kNone, in = kNone;
+      const int rx = cx & rm, ry = cy & rm, rz = cz & rm;
+      if (head) {
+        in = (rx == rkx && ry == rky && rz == rkz) ? rin : root_get_or_create(M, rx, ry, rz);
+        if (in != kNone) leaf = leaf_get_or_create(M, in, inner_index(M, cx, cy, cz), lkx, lky, lkz);
+      }
+      const unsigned hm = (__ballot_sync(gmask, head) & gmask) >> gbase;
+      const unsigned below = hm & ((2u << sl) - 1u);
+      const int src = below ? 31 - __clz(below) : 0;
+      const uint32_t got = __shfl_sync(gmask, leaf, src, W);
+      leaf = below ? got : pleaf;
+      if (hm) {  // remember the root of the highest head
+        const int hl = 31 - __clz(hm);
+        rkx = __shfl_sync(gmask, rx, hl, W);
+        rky = __shfl_sync(gmask, ry, hl, W);
+        rkz = __shfl_sync(gmask, rz, hl, W);
+        rin = __shfl_sync(gmask, in, hl, W);
+      }
+      if (act && leaf != kNone) {
+        const uint32_t ci = leaf_index(M, cx, cy, cz);
+        cell_mark_on(M, leaf, ci);
+        int32_t* cp = reinterpret_cast<int32_t*>(M.ldata) + size_t(leaf) * M.lsize + ci;
+        const int32_t w = *cp;
+        if (cell_id(w) != u) {
+          *cp = cell_pack(max(wrap_add(cell_prob(w), miss), cmin), u);
+          updated++;
+        }
+        visited++;
+      }
+      const uint32_t rem = m - base;
+      const int last = static_cast<int>(rem < W ? rem : W) - 1;
+      pkx = __shfl_sync(gmask, lkx, last, W);
+      pky = __shfl_sync(gmask, lky, last, W);
+      pkz = __shfl_sync(gmask, lkz, last, W);
+      pleaf = __shfl_sync(gmask, leaf, last, W);
+      axis_advance(X, two_m);
+      axis_advance(Y, two_m);
+      axis_advance(Z, two_m);
+    }
+  }
+  visited = __reduce_add_sync(0xffffffffu, visited);
+  updated = __reduce_add_sync(0xffffffffu, updated);
+  if (lane == 0 && visited) {
+    unsigned long long* st = reinterpret_cast<unsigned long long*>(M.ctr + C_STATS);
+    atomicAdd(st + S_VISITED, static_cast<unsigned long long>(visited));
+    atomicAdd(st + S_UPDATED, static_cast<unsigned long long>(updated));
+  }
+}
+
+// isOccupied / isUnknown / isFree (probabilistic_map.cpp:56-75).
+__global__ void k_query(DMap M, const int32_t* __restrict__ xyz, uint32_t n, int mode,
+                        int32_t thr, uint8_t* __restrict__ out) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int x = xyz[3 * i], y = xyz[3 * i + 1], z = xyz[3 * i + 2];
+  const uint32_t lf = leaf_of(M, x, y, z, false);
+  bool have = false;
+  int32_t p = 0;
+  if (lf != kNone) {
+    const uint32_t ci = leaf_index(M, x, y, z);
+    if (cell_is_on(M, lf, ci)) {
+      have = true;
+      p = cell_prob(reinterpret_cast<const int32_t*>(M.ldata)[size_t(lf) * M.lsize + ci]);
+    }
+  }
+  uint8_t r;
+  if (mode == 0)
+    r = have && p > thr;
+  else if (mode == 1)
+    r = have ? p == thr : 1;
+  else
+    r = have && p < thr;
+  out[i] = r;
+}
+
+// ComputeRay for a batch of rays (probabilistic_map.hpp:13-19), thread per ray.
+__global__ void k_compute_rays(const int32_t* __restrict__ o, const int32_t* __restrict__ e,
+                               uint32_t n, uint32_t* __restrict__ len,
+                               const unsigned long long* __restrict__ off,
+                               int32_t* __restrict__ out) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int ox = o[3 * i], oy = o[3 * i + 1], oz = o[3 * i + 2];
+  const int dx = e[3 * i] - ox, dy = e[3 * i + 1] - oy, dz = e[3 * i + 2] - oz;
+  const uint32_t ax = abs(dx), ay = abs(dy), az = abs(dz);
+  const uint32_t m = max(ax, max(ay, az));
+  if (len) len[i] = m;
+  if (!out || m == 0 || m >= kMaxRayCells) return;
+  const uint32_t two_m = 2u * m;
+  const float rtm = __frcp_rn(static_cast<float>(two_m));
+  AxisStep X, Y, Z;
+  axis_init(X, ax, m, two_m, rtm, 0, 1);
+  axis_init(Y, ay, m, two_m, rtm, 0, 1);
+  axis_init(Z, az, m, two_m, rtm, 0, 1);
+  int32_t* dst = out + 3 * off[i];
+  for (uint32_t k = 0; k < m; k++) {
+    dst[3 * k + 0] = ox + (dx < 0 ? -int(X.n) : int(X.n));
+    dst[3 * k + 1] = oy + (dy < 0 ? -int(Y.n) : int(Y.n));
+    dst[3 * k + 2] = oz + (dz < 0 ? -int(Z.n) : int(Z.n));
+    axis_advance(X, two_m);
+    axis_advance(Y, two_m);
+    axis_advance(Z, two_m);
+  }
+}
+
+}  // namespace bxg
+
+using namespace bxg;
+
+namespace {
+
+uint32_t next_pow2(uint64_t v) {
+  uint32_t p = 64;
+  while (p < v) p <<= 1;
+  return p;
+}
+
+Opts opts_of(const bxg_pmap_s* pm) {
+  return Opts{pm->opt.prob_miss_log, pm->opt.prob_hit_log, pm->opt.clamp_min_log,
+              pm->opt.clamp_max_log};
+}
+
+// logods(p) = int32_t(1e6 * log(p / (1.0 - p))) (probabilistic_map.hpp:34-36).
+int32_t logods(float p) {
+  return static_cast<int32_t>(1e6 * std::log(p / (1.0 - p)));
+}
+
+void record(bxg_pmap_s* pm, int k) {
+  if ((pm->core.flags & BXG_FLAG_TIMING) && pm->ev[k]) cudaEventRecord(pm->ev[k], pm->core.stream);
+}
+
+int reset_scan_stats(MapCore* m) {
+  BXG_CUDA(m, cudaMemsetAsync(m->ctr.as<uint32_t>() + C_STATS, 0, S_COUNT * 8, m->stream));
+  return BXG_OK;
+}
+
+// Endpoint phase for n staged points (k_endpoints or k_endpoints_kind), then
+// the winners that join the ray list, then the endpoint updates.
+template <class Launch>
+int endpoint_phase(bxg_pmap_s* pm, uint32_t n, int ox, int oy, int oz, Launch&& launch_ep) {
+  MapCore* m = &pm->core;
+  const uint32_t tcap = next_pow2(uint64_t(n) * 2);
+  BXG_CUDA(m, m->s_ep.ensure(size_t(n) * 16));
+  BXG_CUDA(m, m->s_dedup.ensure(size_t(tcap) * 16));
+  // the ray list persists across add-batches until updateFreeCells
+  const uint64_t need = pm->cast_ub + n;
+  BXG_CUDA(m, m->s_cast.ensure_keep(need * 16, pm->cast_ub * 16, m->stream));
+  launch_dedup_clear(m, m->s_dedup.as<uint4>(), tcap);
+  const unsigned blocks = (n + 255) / 256;
+  launch_ep(blocks, m->s_ep.as<int4>(), m->s_dedup.as<uint4>(), tcap - 1);
+  BXG_LAUNCHED(m);
+  record(pm, 1);
+  k_winners<<<blocks, 256, 0, m->stream>>>(m->dm, m->s_ep.as<int4>(), n, m->s_dedup.as<uint4>(),
+                                           tcap - 1, ox, oy, oz, pm->update_count,
+                                           m->s_cast.as<int4>(), uint32_t(m->s_cast.cap / 16));
+  BXG_LAUNCHED(m);
+  record(pm, 2);
+  pm->cast_ub = need;
+  return BXG_OK;
+}
+
+int launch_apply(bxg_pmap_s* pm) {
+  MapCore* m = &pm->core;
+  const unsigned blocks =
+      unsigned(std::min<uint64_t>((pm->cast_ub + 255) / 256, uint64_t(m->sm_count) * 8));
+  if (blocks) {
+    k_apply<<<std::max(blocks, 1u), 256, 0, m->stream>>>(
+        m->dm, m->s_cast.as<int4>(), uint32_t(m->s_cast.cap / 16), pm->update_count,
+        opts_of(pm));
+    BXG_LAUNCHED(m);
+  }
+  return BXG_OK;
+}
+
+int launch_rays(bxg_pmap_s* pm, int ox, int oy, int oz) {
+  MapCore* m = &pm->core;
+  const uint32_t rpw = m->rays_per_warp ? m->rays_per_warp : 1;
+  // 64..256 threads (the kernel's launch bound), a multiple of 32
+  const int bs = m->block_size ? std::min(256, std::max(64, int(m->block_size) & ~31)) : 256;
+  const uint64_t groups_per_block = uint64_t(bs) / (32 / rpw);
+  uint64_t blocks = (pm->cast_ub + groups_per_block - 1) / groups_per_block;
+  blocks = std::min<uint64_t>(blocks, uint64_t(m->sm_count) * (2048 / bs));
+  if (!blocks) return BXG_OK;
+  const Opts o = opts_of(pm);
+  const uint32_t ccap = uint32_t(m->s_cast.cap / 16);
+  switch (rpw) {
+    case 4:
+      k_rays<8><<<unsigned(blocks), bs, 0, m->stream>>>(m->dm, m->s_cast.as<int4>(), ccap, ox, oy, oz,
+                                                        pm->update_count, o.miss, o.cmin);
+      break;
+    case 2:
+      k_rays<16><<<unsigned(blocks), bs, 0, m->stream>>>(m->dm, m->s_cast.as<int4>(), ccap, ox, oy, oz,
+                                                         pm->update_count, o.miss, o.cmin);
+      break;
+    default:
+      k_rays<32><<<unsigned(blocks), bs, 0, m->stream>>>(m->dm, m->s_cast.as<int4>(), ccap, ox, oy, oz,
+                                                         pm->update_count, o.miss, o.cmin);
+      break;
+  }
+  BXG_LAUNCHED(m);
+  return BXG_OK;
+}
+
+// Applies the queued endpoints (if not yet applied) and casts the rays,
+// growing pools and retrying on exhaustion; then ends the scan.
+int finish_scan(bxg_pmap_s* pm, int ox, int oy, int oz, bool cast_rays, uint64_t* ray_cells,
+                bool include_points) {
+  MapCore* m = &pm->core;
+  int st = BXG_OK;
+  for (int attempt = 0; attempt < 12; attempt++) {
+    if (attempt) {
+      // retries recount the ray statistics
+      unsigned long long* s = stats_of(m);
+      BXG_CUDA(m, cudaMemsetAsync(s + S_VISITED, 0, 16, m->stream));
+    }
+    st = launch_apply(pm);
+    if (st) return st;
+    record(pm, 3);
+    if (cast_rays) {
+      st = launch_rays(pm, ox, oy, oz);
+      if (st) return st;
+    }
+    record(pm, 4);
+    uint32_t err = 0;
+    st = core_sync(m, &err);
+    if (st == BXG_OK) break;
+    if (!(err & (ERR_POOL_INNER | ERR_POOL_LEAF | ERR_HASH_FULL))) return st;
+    const int g = core_grow_for(m, err);
+    if (g) return g;
+  }
+  if (st) return st;
+  const unsigned long long* hs = reinterpret_cast<const unsigned long long*>(m->h_ctr + C_STATS);
+  pm->last_stats[0] = hs[S_POINTS];
+  pm->last_stats[1] = m->h_ctr[C_CAST];
+  pm->last_stats[2] = hs[S_VISITED];
+  pm->last_stats[3] = hs[S_UPDATED];
+  pm->last_stats[4] = m->h_ctr[C_LEAF];
+  pm->last_stats[5] = m->launches;
+  if (ray_cells) *ray_cells = (include_points ? hs[S_POINTS] : 0) + hs[S_RAY_LEN];
+  if (m->flags & BXG_FLAG_TIMING) {
+    for (int k = 0; k < 4; k++) {
+      float ms = 0;
+      if (pm->ev[k] && pm->ev[k + 1]) cudaEventElapsedTime(&ms, pm->ev[k], pm->ev[k + 1]);
+      pm->last_times[k] = ms;
+    }
+  }
+  if (cast_rays) {
+    // end of scan: empty the ray list, advance the counter (cpp:301-310)
+    BXG_CUDA(m, cudaMemsetAsync(m->ctr.as<uint32_t>() + C_CAST, 0, 4, m->stream));
+    pm->cast_ub = 0;
+    if (++pm->update_count == 4) pm->update_count = 1;
+    BXG_CUDA(m, cudaStreamSynchronize(m->stream));
+  }
+  return core_maintain(m);
+}
+
+int origin_coord(const MapCore* m, double x, double y, double z, int* c) {
+  c[0] = static_cast<int>(std::floor(x * m->inv_res));
+  c[1] = static_cast<int>(std::floor(y * m->inv_res));
+  c[2] = static_cast<int>(std::floor(z * m->inv_res));
+  return BXG_OK;
+}
+
+template <typename PT>
+int insert_impl(bxg_pmap m_, const PT* xyz, size_t stride, size_t n, const PT* origin,
+                double max_range, uint64_t* ray_cells, bool sync) {
+  if (!m_) return BXG_ERR_INVALID_ARG;
+  bxg_pmap_s* pm = m_;
+  MapCore* m = &pm->core;
+  if (!origin || (n && !xyz) || n >= 0x7FFFFFFFu)
+    return set_error(m, BXG_ERR_INVALID_ARG, "null input or batch too large");
+  if (!stride) stride = 3 * sizeof(PT);
+  cudaSetDevice(m->device);
+  // from = ConvertPoint<Vector3d>(origin): the origin widened to double.
+  const double fx = static_cast<double>(origin[0]), fy = static_cast<double>(origin[1]),
+               fz = static_cast<double>(origin[2]);
+  int o[3];
+  origin_coord(m, fx, fy, fz, o);
+  record(pm, 0);  // the scan's device time starts here
+  int st = reset_scan_stats(m);
+  if (st) return st;
+  if (n) {
+    const void* dpts = nullptr;
+    st = stage_in(m, m->s_in, xyz, stride * (n - 1) + 3 * sizeof(PT), &dpts);
+    if (st) return st;
+    const double mr2 = max_range * max_range;
+    const int keep = (m->flags & BXG_FLAG_KEEP_NONFINITE) ? 1 : 0;
+    st = endpoint_phase(pm, uint32_t(n), o[0], o[1], o[2],
+                        [&](unsigned blocks, int4* ep, uint4* tab, uint32_t tmask) {
+                          k_endpoints<PT><<<blocks, 256, 0, m->stream>>>(
+                              m->dm, static_cast<const uint8_t*>(dpts), stride, uint32_t(n), fx,
+                              fy, fz, max_range, mr2, m->inv_res, keep, ep, tab, tmask);
+                        });
+    if (st) return st;
+  }
+  if (!sync) {
+    // asynchronous form: no retry; pools must have room (see core_maintain)
+    st = launch_apply(pm);
+    if (st) return st;
+    st = launch_rays(pm, o[0], o[1], o[2]);
+    if (st) return st;
+    BXG_CUDA(m, cudaMemsetAsync(m->ctr.as<uint32_t>() + C_CAST, 0, 4, m->stream));
+    pm->cast_ub = 0;
+    if (++pm->update_count == 4) pm->update_count = 1;
+    return BXG_OK;
+  }
+  return finish_scan(pm, o[0], o[1], o[2], true, ray_cells, true);
+}
+
+int add_points(bxg_pmap m_, const double* xyz, size_t n, int kind) {
+  if (!m_) return BXG_ERR_INVALID_ARG;
+  bxg_pmap_s* pm = m_;
+  MapCore* m = &pm->core;
+  if (!n) return BXG_OK;
+  if (!xyz || n >= 0x7FFFFFFFu) return set_error(m, BXG_ERR_INVALID_ARG, "null input");
+  cudaSetDevice(m->device);
+  record(pm, 0);
+  if (pm->cast_ub == 0) {
+    int st = reset_scan_stats(m);
+    if (st) return st;
+  }
+  const void* dpts = nullptr;
+  int st = stage_in(m, m->s_in, xyz, n * 24, &dpts);
+  if (st) return st;
+  st = endpoint_phase(pm, uint32_t(n), 0, 0, 0,
+                      [&](unsigned blocks, int4* ep, uint4* tab, uint32_t tmask) {
+                        k_endpoints_kind<<<blocks, 256, 0, m->stream>>>(
+                            m->dm, static_cast<const double*>(dpts), uint32_t(n), kind,
+                            m->inv_res, ep, tab, tmask);
+                      });
+  if (st) return st;
+  // apply now so that queries see the endpoint updates, as in the reference
+  return finish_scan(pm, 0, 0, 0, false, nullptr, false);
+}
+
+int query(bxg_pmap m_, const int32_t* xyz, size_t n, uint8_t* out, int mode) {
+  if (!m_) return BXG_ERR_INVALID_ARG;
+  MapCore* m = &m_->core;
+  if (!n) return BXG_OK;
+  if (!xyz || !out || n >= 0x7FFFFFFFu) return set_error(m, BXG_ERR_INVALID_ARG, "null pointer");
+  cudaSetDevice(m->device);
+  const void* dxyz = nullptr;
+  void* dout = nullptr;
+  int st = stage_in(m, m->s_in, xyz, n * 12, &dxyz);
+  if (st) return st;
+  st = stage_out(m, m->s_out, out, n, &dout);
+  if (st) return st;
+  k_query<<<unsigned((n + 255) / 256), 256, 0, m->stream>>>(
+      m->dm, static_cast<const int32_t*>(dxyz), uint32_t(n), mode,
+      m_->opt.occupancy_threshold_log, static_cast<uint8_t*>(dout));
+  BXG_LAUNCHED(m);
+  st = stage_out_finish(m, out, dout, n);
+  if (st) return st;
+  BXG_CUDA(m, cudaStreamSynchronize(m->stream));
+  return BXG_OK;
+}
+
+}  // namespace
+
+namespace bxg {
+const MapCore* core_of_handle(const void* handle) {
+  // Both handle types hold their MapCore as first member.
+  return reinterpret_cast<const MapCore*>(handle);
+}
+}  // namespace bxg
+
+extern "C" {
+
+int bxg_pmap_create(bxg_pmap* out, double resolution, const bxg_config* cfg) {
+  if (!out) return BXG_ERR_INVALID_ARG;
+  *out = nullptr;
+  bxg_pmap pm = new bxg_pmap_s();
+  // ProbabilisticMap's grid is VoxelGrid<CellT>(resolution) with default bits.
+  int st = core_init(&pm->core, resolution, 2, 3, 4, cfg);
+  if (st) {
+    set_create_error(pm->core.err);
+    delete pm;
+    return st;
+  }
+  pm->opt.prob_miss_log = logods(0.4f);
+  pm->opt.prob_hit_log = logods(0.7f);
+  pm->opt.clamp_min_log = logods(0.12f);
+  pm->opt.clamp_max_log = logods(0.97f);
+  pm->opt.occupancy_threshold_log = logods(0.5f);
+  if (pm->core.flags & BXG_FLAG_TIMING)
+    for (auto& e : pm->ev) cudaEventCreate(&e);
+  *out = pm;
+  return BXG_OK;
+}
+
+int bxg_pmap_destroy(bxg_pmap m) {
+  delete m;
+  return BXG_OK;
+}
+
+int bxg_pmap_get_options(bxg_pmap m, bxg_pmap_options* out) {
+  if (!m || !out) return BXG_ERR_INVALID_ARG;
+  *out = m->opt;
+  return BXG_OK;
+}
+
+int bxg_pmap_set_options(bxg_pmap m, const bxg_pmap_options* opt) {
+  if (!m || !opt) return BXG_ERR_INVALID_ARG;
+  m->opt = *opt;
+  return BXG_OK;
+}
+
+int bxg_pmap_insert_point_cloud_f32(bxg_pmap m, const float* xyz, size_t stride, size_t n,
+                                    const float origin[3], double max_range,
+                                    uint64_t* ray_cells) {
+  return insert_impl(m, xyz, stride, n, origin, max_range, ray_cells, true);
+}
+
+int bxg_pmap_insert_point_cloud_f64(bxg_pmap m, const double* xyz, size_t stride, size_t n,
+                                    const double origin[3], double max_range,
+                                    uint64_t* ray_cells) {
+  return insert_impl(m, xyz, stride, n, origin, max_range, ray_cells, true);
+}
+
+int bxg_pmap_insert_point_cloud_f32_async(bxg_pmap m, const float* xyz, size_t stride,
+                                          size_t n, const float origin[3], double max_range) {
+  return insert_impl(m, xyz, stride, n, origin, max_range, nullptr, false);
+}
+
+int bxg_pmap_add_hit_points(bxg_pmap m, const double* xyz, size_t n) {
+  return add_points(m, xyz, n, EP_HIT);
+}
+
+int bxg_pmap_add_miss_points(bxg_pmap m, const double* xyz, size_t n) {
+  return add_points(m, xyz, n, EP_MISS);
+}
+
+int bxg_pmap_update_free_cells(bxg_pmap pm, const double origin[3], uint64_t* ray_cells) {
+  if (!pm || !origin) return BXG_ERR_INVALID_ARG;
+  MapCore* m = &pm->core;
+  cudaSetDevice(m->device);
+  int o[3];
+  origin_coord(m, origin[0], origin[1], origin[2], o);
+  // the ray lengths counted at add time were measured from (0,0,0); recount
+  // them for this origin on the host-visible path
+  if (ray_cells) {
+    int st = core_sync(m);
+    if (st) return st;
+  }
+  const uint32_t n_cast = m->h_ctr[C_CAST];
+  uint64_t len = 0;
+  if (ray_cells && n_cast) {
+    std::vector<int4> h(n_cast);
+    BXG_CUDA(m, cudaMemcpy(h.data(), m->s_cast.p, size_t(n_cast) * 16, cudaMemcpyDeviceToHost));
+    for (const int4& e : h) {
+      const int64_t dx = std::llabs(int64_t(e.x) - o[0]), dy = std::llabs(int64_t(e.y) - o[1]),
+                    dz = std::llabs(int64_t(e.z) - o[2]);
+      len += uint64_t(std::max(dx, std::max(dy, dz)));
+    }
+  }
+  const int st = finish_scan(pm, o[0], o[1], o[2], true, nullptr, false);
+  if (st) return st;
+  if (ray_cells) *ray_cells = len;
+  return BXG_OK;
+}
+
+int bxg_pmap_is_occupied(bxg_pmap m, const int32_t* xyz, size_t n, uint8_t* out) {
+  return query(m, xyz, n, out, 0);
+}
+int bxg_pmap_is_unknown(bxg_pmap m, const int32_t* xyz, size_t n, uint8_t* out) {
+  return query(m, xyz, n, out, 1);
+}
+int bxg_pmap_is_free(bxg_pmap m, const int32_t* xyz, size_t n, uint8_t* out) {
+  return query(m, xyz, n, out, 2);
+}
+
+int bxg_pmap_get_occupied(bxg_pmap m, int32_t* out_xyz, size_t cap, size_t* n_out) {
+  if (!m) return BXG_ERR_INVALID_ARG;
+  cudaSetDevice(m->core.device);
+  return core_dump(&m->core, out_xyz, nullptr, cap, n_out, 1, m->opt.occupancy_threshold_log);
+}
+
+int bxg_pmap_get_free(bxg_pmap m, int32_t* out_xyz, size_t cap, size_t* n_out) {
+  if (!m) return BXG_ERR_INVALID_ARG;
+  cudaSetDevice(m->core.device);
+  return core_dump(&m->core, out_xyz, nullptr, cap, n_out, 2, m->opt.occupancy_threshold_log);
+}
+
+int bxg_pmap_dump(bxg_pmap m, int32_t* out_xyz, int32_t* out_cells, size_t cap, size_t* n_out) {
+  if (!m) return BXG_ERR_INVALID_ARG;
+  cudaSetDevice(m->core.device);
+  return core_dump(&m->core, out_xyz, out_cells, cap, n_out, 0, 0);
+}
+
+int bxg_pmap_active_cells(bxg_pmap m, size_t* out) {
+  if (!m) return BXG_ERR_INVALID_ARG;
+  cudaSetDevice(m->core.device);
+  return core_active_cells(&m->core, out);
+}
+
+int bxg_pmap_node_counts(bxg_pmap m, size_t* roots, size_t* leaves) {
+  if (!m) return BXG_ERR_INVALID_ARG;
+  cudaSetDevice(m->core.device);
+  return core_node_counts(&m->core, roots, leaves);
+}
+
+int bxg_pmap_mem_usage(bxg_pmap m, size_t* out) {
+  if (!m || !out) return BXG_ERR_INVALID_ARG;
+  *out = core_mem_usage(&m->core);
+  return BXG_OK;
+}
+
+int bxg_pmap_update_count(bxg_pmap m, int* out) {
+  if (!m || !out) return BXG_ERR_INVALID_ARG;
+  *out = m->update_count;
+  return BXG_OK;
+}
+
+int bxg_pmap_clear(bxg_pmap m) {
+  if (!m) return BXG_ERR_INVALID_ARG;
+  cudaSetDevice(m->core.device);
+  m->cast_ub = 0;
+  return core_clear(&m->core);
+}
+
+int bxg_pmap_synchronize(bxg_pmap m) {
+  if (!m) return BXG_ERR_INVALID_ARG;
+  cudaSetDevice(m->core.device);
+  int st = core_sync(&m->core);
+  if (st) return st;
+  return core_maintain(&m->core);
+}
+
+int bxg_pmap_last_stats(bxg_pmap m, uint64_t out[8]) {
+  if (!m || !out) return BXG_ERR_INVALID_ARG;
+  std::memcpy(out, m->last_stats, sizeof(m->last_stats));
+  return BXG_OK;
+}
+
+int bxg_pmap_kernel_times(bxg_pmap m, float out[4]) {
+  if (!m || !out) return BXG_ERR_INVALID_ARG;
+  std::memcpy(out, m->last_times, sizeof(m->last_times));
+  return BXG_OK;
+}
+
+void* bxg_pmap_stream(bxg_pmap m) { return m ? static_cast<void*>(m->core.stream) : nullptr; }
+
+int bxg_compute_rays(const int32_t* origin_xyz, const int32_t* end_xyz, size_t n,
+                     uint32_t* out_len, const uint64_t* offsets, int32_t* out_xyz) {
+  if (!n) return BXG_OK;
+  if (!origin_xyz || !end_xyz || n >= 0x7FFFFFFFu) return BXG_ERR_INVALID_ARG;
+  if (out_xyz && !offsets) return BXG_ERR_INVALID_ARG;
+  MapCore tmp;
+  tmp.device = -1;
+  cudaGetDevice(&tmp.device);
+  cudaStream_t s = nullptr;
+  BXG_CUDA(&tmp, cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  tmp.stream = s;
+  tmp.own_stream = true;
+  const void *dO = nullptr, *dE = nullptr, *dOff = nullptr;
+  void *dLen = nullptr, *dOut = nullptr;
+  int st = stage_in(&tmp, tmp.s_in, origin_xyz, n * 12, &dO);
+  if (!st) st = stage_in(&tmp, tmp.s_in2, end_xyz, n * 12, &dE);
+  if (!st) st = stage_out(&tmp, tmp.s_out, out_len, n * 4, &dLen);
+  size_t total = 0;
+  if (!st && out_xyz) {
+    // total cells = offsets[n-1] + length of the last ray
+    uint64_t last_off = 0;
+    if (is_device_ptr(offsets))
+      cudaMemcpy(&last_off, offsets + (n - 1), 8, cudaMemcpyDeviceToHost);
+    else
+      last_off = offsets[n - 1];
+    int32_t lo[3], le[3];
+    if (is_device_ptr(origin_xyz)) {
+      cudaMemcpy(lo, origin_xyz + 3 * (n - 1), 12, cudaMemcpyDeviceToHost);
+      cudaMemcpy(le, end_xyz + 3 * (n - 1), 12, cudaMemcpyDeviceToHost);
+    } else {
+      std::memcpy(lo, origin_xyz + 3 * (n - 1), 12);
+      std::memcpy(le, end_xyz + 3 * (n - 1), 12);
+    }
+    const uint64_t ml = std::max({std::llabs(int64_t(le[0]) - lo[0]),
+                                  std::llabs(int64_t(le[1]) - lo[1]),
+                                  std::llabs(int64_t(le[2]) - lo[2])});
+    total = size_t(last_off + ml);
+    st = stage_in(&tmp, tmp.s_ep, offsets, n * 8, &dOff);
+    if (!st) st = stage_out(&tmp, tmp.s_out2, out_xyz, total * 12, &dOut);
+  }
+  if (st) return st;
+  k_compute_rays<<<unsigned((n + 255) / 256), 256, 0, s>>>(
+      static_cast<const int32_t*>(dO), static_cast<const int32_t*>(dE), uint32_t(n),
+      static_cast<uint32_t*>(dLen), static_cast<const unsigned long long*>(dOff),
+      static_cast<int32_t*>(dOut));
+  BXG_LAUNCHED(&tmp);
+  if (dLen) st = stage_out_finish(&tmp, out_len, dLen, n * 4);
+  if (!st && dOut) st = stage_out_finish(&tmp, out_xyz, dOut, total * 12);
+  if (st) return st;
+  BXG_CUDA(&tmp, cudaStreamSynchronize(s));
+  return BXG_OK;
+}
+
+}  // extern "C"

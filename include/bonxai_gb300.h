@@ -1,0 +1,234 @@
+/*
+ * bonxai_gb300 -- C ABI of the GB300 (sm_103a) sparse voxel grid.
+ *
+ * This is the drop-in boundary: the C++ headers include/bonxai/bonxai.hpp and
+ * include/bonxai_map/probabilistic_map.hpp re-create the reference's classes
+ * on top of these functions, and any other language binds them through its FFI
+ * (plain pointers and sizes, no C++ or torch types).
+ *
+ * Every entry point is named after the reference interface it replaces, cited
+ * as path:line in the reference repository (bonxai_core/include/bonxai/ and
+ * bonxai_map/). The reference is a header-only C++ library with no C ABI of its
+ * own; each batch function here performs, in one GPU pass, what a loop of the
+ * cited scalar C++ calls does, with the same results.
+ *
+ * Pointers: every input/output array may be host memory (pageable or pinned)
+ * or device memory; the library checks with cudaPointerGetAttributes and
+ * stages host arrays through the handle's device scratch. Coordinates are
+ * packed int32 x,y,z triples. Points are packed x,y,z of float or double with
+ * an optional byte stride (e.g. 16 for pcl::PointXYZ).
+ *
+ * Errors: every function returns a bxg_status. The reference throws
+ * std::runtime_error or returns nullptr (bonxai.hpp:399-401,
+ * serialization.hpp:128-130); here the text of the last error of a handle is
+ * kept and returned by bxg_last_error(). A failed call leaves the map usable.
+ *
+ * Threading: calls on one handle are serialised by the caller (the reference's
+ * writers are not thread-safe either, README.md:128-133); different handles
+ * may be used from different host threads. Each handle runs on its own CUDA
+ * stream (or the one given in bxg_config). Synchronous calls return after the
+ * GPU work completes, like the reference's calls.
+ */
+#ifndef BONXAI_GB300_H
+#define BONXAI_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  BXG_OK = 0,
+  BXG_ERR_INVALID_ARG = 1,
+  BXG_ERR_OUT_OF_POOL = 2,    /* node pools reached the configured HBM budget */
+  BXG_ERR_HASH_FULL = 3,      /* root hash could not grow within the budget */
+  BXG_ERR_WAIT_TIMEOUT = 4,   /* a bounded device-side wait gave up */
+  BXG_ERR_CUDA = 5,           /* a CUDA runtime call failed */
+  BXG_ERR_NO_DEVICE = 6,      /* no usable CUDA device */
+  BXG_ERR_CAPACITY = 7        /* caller's output buffer too small (size returned) */
+} bxg_status;
+
+/* Pool/stream configuration; zero-initialise and set what you need. */
+typedef struct {
+  size_t pool_budget_bytes; /* max device bytes for hash+inner+leaf pools; 0 = 16 GiB */
+  uint32_t initial_leaves;  /* leaf slots allocated up front; 0 = 4096 */
+  uint32_t initial_inners;  /* inner slots allocated up front; 0 = 1024 */
+  uint32_t hash_buckets;    /* root hash buckets (power of two); 0 = 4096 */
+  float hash_load_factor;   /* grow the root hash above this load; 0 = 0.5 */
+  int device;               /* CUDA device ordinal; -1 = current */
+  void* stream;             /* cudaStream_t to run on; NULL = a stream of its own */
+  uint32_t rays_per_warp;   /* ray kernel: rays per warp 1, 2 or 4; 0 = autotuned */
+  uint32_t block_size;      /* ray kernel threads per block; 0 = autotuned */
+  uint32_t flags;           /* BXG_FLAG_* */
+} bxg_config;
+
+/* Drop points with a NaN or infinite coordinate before insertion, as the
+ * reference's ROS node does before calling insertPointCloud
+ * (bonxai_ros/src/bonxai_server.cpp:147-154). Default on. */
+#define BXG_FLAG_KEEP_NONFINITE 1u
+/* Record CUDA events around each kernel (see bxg_pmap_kernel_times). */
+#define BXG_FLAG_TIMING 2u
+
+void bxg_config_default(bxg_config* cfg);
+const char* bxg_status_string(int status);
+/* Version of this library as major*10000 + minor*100 + patch. */
+int bxg_version(void);
+
+/* ========================================================================
+ * VoxelGrid<T>  (bonxai_core/include/bonxai/bonxai.hpp:114-333)
+ * ======================================================================== */
+typedef struct bxg_grid_s* bxg_grid;
+
+/* VoxelGrid(double voxel_size, uint8_t inner_bits=2, uint8_t leaf_bits=3)
+ * (bonxai.hpp:138,389-402). value_bytes = sizeof(T): 1, 2, 4, 8 or 0 for
+ * BinaryVoxelGrid = VoxelGrid<EmptyVoxel> (bonxai.hpp:335). inner_bits in
+ * [1,4], leaf_bits in [1,5]; the reference rejects bits < 1 the same way. */
+int bxg_grid_create(bxg_grid* out, double voxel_size, int inner_bits, int leaf_bits,
+                    size_t value_bytes, const bxg_config* cfg);
+int bxg_grid_destroy(bxg_grid g);
+const char* bxg_last_error(const void* handle);
+
+/* posToCoord(x,y,z) = floor(x * (1.0/voxel_size)) per axis in double
+ * (bonxai.hpp:404-410) for n double points. */
+int bxg_grid_pos_to_coord(bxg_grid g, const double* xyz, size_t n, int32_t* out_xyz);
+
+/* Accessor::setValue(coord, value) for items 0..n-1 in order
+ * (bonxai.hpp:449-466): a cell written several times keeps the value of the
+ * highest index. was_on (optional) gets each call's return value: the cell's
+ * state before that call. */
+int bxg_grid_set_values(bxg_grid g, const int32_t* xyz, const void* values, size_t n,
+                        uint8_t* was_on);
+/* setValue(posToCoord(p), value) with float/double points (stride in bytes, 0 =
+ * packed); the grid computes posToCoord in double. */
+int bxg_grid_set_values_at_points_f32(bxg_grid g, const float* xyz, size_t stride, size_t n,
+                                      const void* values);
+int bxg_grid_set_values_at_points_f64(bxg_grid g, const double* xyz, size_t stride, size_t n,
+                                      const void* values);
+
+/* Accessor::value(coord, create_if_missing) (bonxai.hpp:469-494) and
+ * ConstAccessor::value (bonxai.hpp:496-516): found[i] = 1 when the cell exists
+ * (or was created, which sets it to T{}); out receives the value (T{} when not
+ * found). Either output may be NULL. */
+int bxg_grid_get_values(bxg_grid g, const int32_t* xyz, size_t n, void* out_values,
+                        uint8_t* found, int create_if_missing);
+/* setCellOn(coord, default_value) (bonxai.hpp:537-553). */
+int bxg_grid_set_cells_on(bxg_grid g, const int32_t* xyz, size_t n, const void* default_value,
+                          uint8_t* was_on);
+/* setCellOff(coord) (bonxai.hpp:556-569). */
+int bxg_grid_set_cells_off(bxg_grid g, const int32_t* xyz, size_t n, uint8_t* was_on);
+/* ConstAccessor::isCellOn(coord) (bonxai.hpp:518-534). */
+int bxg_grid_is_cell_on(bxg_grid g, const int32_t* xyz, size_t n, uint8_t* out);
+
+/* activeCellsCount() (bonxai.hpp:689-701). */
+int bxg_grid_active_cells(bxg_grid g, size_t* out);
+/* Node counts: roots (root map entries), inner nodes, leaves in use. */
+int bxg_grid_node_counts(bxg_grid g, size_t* roots, size_t* leaves);
+/* memUsage() (bonxai.hpp:649-676): device bytes held by this grid's pools. */
+int bxg_grid_mem_usage(bxg_grid g, size_t* out);
+/* forEachCell (bonxai.hpp:703-743) as a dump: every active cell's coordinate
+ * and value, in an unspecified order (the reference's order is that of an
+ * unordered_map). Writes at most cap items, *n_out = active count; returns
+ * BXG_ERR_CAPACITY if cap was too small. */
+int bxg_grid_dump(bxg_grid g, int32_t* out_xyz, void* out_values, size_t cap, size_t* n_out);
+/* clear(CLEAR_MEMORY = 0 | SET_ALL_CELLS_OFF = 1) (bonxai.hpp:678-687). */
+int bxg_grid_clear(bxg_grid g, int option);
+/* releaseUnusedMemory() (bonxai.hpp:367-387): leaves with every cell off go
+ * back to the pool, and roots with no leaf leave the root map. */
+int bxg_grid_release_unused(bxg_grid g);
+int bxg_grid_synchronize(bxg_grid g);
+
+/* ========================================================================
+ * ProbabilisticMap  (bonxai_map/include/bonxai_map/probabilistic_map.hpp:27-137)
+ * ======================================================================== */
+typedef struct bxg_pmap_s* bxg_pmap;
+
+/* Options (probabilistic_map.hpp:56-64), int32 fixed-point log-odds x 1e6. */
+typedef struct {
+  int32_t prob_miss_log;           /* logods(0.4f)  = -405465 */
+  int32_t prob_hit_log;            /* logods(0.7f)  =  847297 */
+  int32_t clamp_min_log;           /* logods(0.12f) = -1992430 */
+  int32_t clamp_max_log;           /* logods(0.97f) = 3476099 */
+  int32_t occupancy_threshold_log; /* logods(0.5)   = 0 */
+} bxg_pmap_options;
+
+/* ProbabilisticMap(double resolution) (probabilistic_map.hpp:68,
+ * probabilistic_map.cpp:12-14), default Options, scan counter 1. */
+int bxg_pmap_create(bxg_pmap* out, double resolution, const bxg_config* cfg);
+int bxg_pmap_destroy(bxg_pmap m);
+/* options() / setOptions() (probabilistic_map.cpp:20-28). */
+int bxg_pmap_get_options(bxg_pmap m, bxg_pmap_options* out);
+int bxg_pmap_set_options(bxg_pmap m, const bxg_pmap_options* opt);
+
+/* insertPointCloud(points, origin, max_range) (probabilistic_map.hpp:141-160):
+ * n points of float (or double) x,y,z with the given byte stride (0 = packed),
+ * origin of the same type. Bit-exact with the reference: endpoint math in
+ * double without contraction, the per-scan update_id gate, Bresenham rays that
+ * include the origin cell and exclude the endpoint, one miss update per ray
+ * cell per scan. Synchronous. ray_cells (optional) receives
+ * V = points + sum of cast ray lengths. */
+int bxg_pmap_insert_point_cloud_f32(bxg_pmap m, const float* xyz, size_t stride, size_t n,
+                                    const float origin[3], double max_range,
+                                    uint64_t* ray_cells);
+int bxg_pmap_insert_point_cloud_f64(bxg_pmap m, const double* xyz, size_t stride, size_t n,
+                                    const double origin[3], double max_range,
+                                    uint64_t* ray_cells);
+/* Same, asynchronous on the handle's stream: returns after enqueueing. Errors
+ * of the device phases are reported by the next synchronous call or by
+ * bxg_pmap_synchronize. */
+int bxg_pmap_insert_point_cloud_f32_async(bxg_pmap m, const float* xyz, size_t stride,
+                                          size_t n, const float origin[3], double max_range);
+
+/* addHitPoint / addMissPoint for n double points, in order
+ * (probabilistic_map.hpp:98,103, probabilistic_map.cpp:30-54). The cells are
+ * updated immediately; their rays are cast by bxg_pmap_update_free_cells. */
+int bxg_pmap_add_hit_points(bxg_pmap m, const double* xyz, size_t n);
+int bxg_pmap_add_miss_points(bxg_pmap m, const double* xyz, size_t n);
+/* updateFreeCells(origin) (probabilistic_map.hpp:136, probabilistic_map.cpp:77-106;
+ * private in the reference, public here): casts the queued rays, then
+ * advances the scan counter 1 -> 2 -> 3 -> 1. ray_cells optional. */
+int bxg_pmap_update_free_cells(bxg_pmap m, const double origin[3], uint64_t* ray_cells);
+
+/* isOccupied / isUnknown / isFree (probabilistic_map.cpp:56-75) for n
+ * coordinates; out[i] = 0/1. */
+int bxg_pmap_is_occupied(bxg_pmap m, const int32_t* xyz, size_t n, uint8_t* out);
+int bxg_pmap_is_unknown(bxg_pmap m, const int32_t* xyz, size_t n, uint8_t* out);
+int bxg_pmap_is_free(bxg_pmap m, const int32_t* xyz, size_t n, uint8_t* out);
+/* getOccupiedVoxels / getFreeVoxels (probabilistic_map.cpp:108-126), unordered. */
+int bxg_pmap_get_occupied(bxg_pmap m, int32_t* out_xyz, size_t cap, size_t* n_out);
+int bxg_pmap_get_free(bxg_pmap m, int32_t* out_xyz, size_t cap, size_t* n_out);
+/* grid().forEachCell over the map (bonxai.hpp:703-743): coordinates and the
+ * packed 4-byte CellT words (update_id in bits 0-3, probability_log in bits
+ * 4-31, the layout GCC gives probabilistic_map.hpp:44-53). */
+int bxg_pmap_dump(bxg_pmap m, int32_t* out_xyz, int32_t* out_cells, size_t cap,
+                  size_t* n_out);
+int bxg_pmap_active_cells(bxg_pmap m, size_t* out);
+int bxg_pmap_node_counts(bxg_pmap m, size_t* roots, size_t* leaves);
+int bxg_pmap_mem_usage(bxg_pmap m, size_t* out);
+/* The scan counter (_update_count, probabilistic_map.hpp:129): 1, 2 or 3. */
+int bxg_pmap_update_count(bxg_pmap m, int* out);
+/* grid().clear(CLEAR_MEMORY): drops every cell; options and counter kept. */
+int bxg_pmap_clear(bxg_pmap m);
+int bxg_pmap_synchronize(bxg_pmap m);
+/* Statistics of the last scan: [0] points, [1] cast rays, [2] ray cells
+ * visited, [3] cells updated by rays, [4] new leaves, [5] kernel launches. */
+int bxg_pmap_last_stats(bxg_pmap m, uint64_t out[8]);
+/* With BXG_FLAG_TIMING: device milliseconds of each phase of the last scan,
+ * measured with CUDA events on the handle's stream: [0] endpoints,
+ * [1] endpoint winners, [2] endpoint update, [3] rays. */
+int bxg_pmap_kernel_times(bxg_pmap m, float out[4]);
+/* The CUDA stream the handle runs on (a cudaStream_t). */
+void* bxg_pmap_stream(bxg_pmap m);
+
+/* ComputeRay(origin, end) (probabilistic_map.hpp:13-19,162-203) on the GPU for
+ * n rays: out_len[i] = ray length; cells of ray i are written at
+ * out_xyz[3*(offsets[i] + k)] when out_xyz != NULL, offsets = exclusive
+ * prefix sum of the lengths (computed by the caller from out_len). */
+int bxg_compute_rays(const int32_t* origin_xyz, const int32_t* end_xyz, size_t n,
+                     uint32_t* out_len, const uint64_t* offsets, int32_t* out_xyz);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BONXAI_GB300_H */

@@ -1,0 +1,215 @@
+"""GPU ProbabilisticMap vs the CPU oracle, bit-exact (cells, packed CellT
+words, ray-cell totals, query answers)."""
+import numpy as np
+import pytest
+import torch
+
+from conftest import golden
+from bonxai_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+
+def assert_same_map(gmap, omap):
+    gx, gc = gmap.dump()
+    ox, oc = omap.dump()
+    assert len(gx) == len(ox), (len(gx), len(ox))
+    assert np.array_equal(gx, ox)
+    bad = np.nonzero(gc != oc)[0]
+    assert len(bad) == 0, (len(bad), gx[bad[:5]], gc[bad[:5]], oc[bad[:5]])
+
+
+def test_golden_lidar(gpu):
+    g = golden("pmap_lidar.npz")
+    m = gpu.ProbabilisticMap(float(g["resolution"]))
+    for k in range(len(g["points"])):
+        v = m.insert_point_cloud(g["points"][k], g["origins"][k], float(g["max_range"]))
+        assert v == g["v"][k]
+        if k == 2:
+            xyz, c = m.dump()
+            assert np.array_equal(xyz, g["xyz3"]) and np.array_equal(c, g["cells3"])
+    xyz, c = m.dump()
+    assert np.array_equal(xyz, g["xyz8"]) and np.array_equal(c, g["cells8"])
+    assert np.array_equal(m.is_occupied(g["query"]), g["occ"])
+    assert np.array_equal(m.is_unknown(g["query"]), g["unk"])
+    assert np.array_equal(m.is_free(g["query"]), g["fre"])
+    assert np.array_equal(m.get_occupied_voxels(), g["occupied"])
+    assert np.array_equal(m.get_free_voxels(), g["free"])
+
+
+def test_golden_repeat(gpu):
+    g = golden("pmap_repeat.npz")
+    m = gpu.ProbabilisticMap(float(g["resolution"]))
+    vs = [m.insert_point_cloud(g["points"], g["origin"], float(g["max_range"]))
+          for _ in range(7)]
+    assert vs == list(g["v"])
+    assert m.update_count == 1 + 7 % 3
+    xyz, c = m.dump()
+    assert np.array_equal(xyz, g["xyz"]) and np.array_equal(c, g["cells"])
+
+
+def test_golden_add_points(gpu):
+    g = golden("pmap_addpts.npz")
+    m = gpu.ProbabilisticMap(float(g["resolution"]))
+    for k in range(len(g["hits"])):
+        m.add_hit_points(g["hits"][k])
+        m.add_miss_points(g["misses"][k])
+        assert m.update_free_cells(g["origins"][k]) == g["ray_cells"][k]
+    xyz, c = m.dump()
+    assert np.array_equal(xyz, g["xyz"]) and np.array_equal(c, g["cells"])
+
+
+@pytest.mark.parametrize("rpw", [1, 2, 4])
+def test_lidar_scans_vs_oracle(gpu, port, rpw):
+    scene = synth.LidarScene()
+    m = gpu.ProbabilisticMap(scene.resolution, gpu.Config(rays_per_warp=rpw))
+    o = port.pmap(scene.resolution)
+    for k in range(5):
+        pts, org = scene.scan(k, n_points=16384)
+        assert m.insert_point_cloud(pts, org, scene.max_range) == o.insert(pts, org, scene.max_range)
+    assert_same_map(m, o)
+
+
+def test_depth_frames_vs_oracle(gpu, port):
+    room = synth.DepthRoom()
+    m = gpu.ProbabilisticMap(room.resolution)
+    o = port.pmap(room.resolution)
+    for k in range(4):
+        pts, org = room.frame(k, subsample=16)
+        assert m.insert_point_cloud(pts, org, room.max_range) == o.insert(pts, org, room.max_range)
+    assert_same_map(m, o)
+    xyz, _ = o.dump()
+    q = synth.lookup_coords(xyz.min(0), xyz.max(0), 200000, seed=1)
+    occ, unk, fre = o.query(q)
+    assert np.array_equal(m.is_occupied(q), occ)
+    assert np.array_equal(m.is_unknown(q), unk)
+    assert np.array_equal(m.is_free(q), fre)
+
+
+def test_device_resident_points_and_stride(gpu, port):
+    scene = synth.LidarScene()
+    pts, org = scene.scan(1, n_points=8192)
+    m1 = gpu.ProbabilisticMap(0.1)
+    m1.insert_point_cloud(torch.from_numpy(pts).cuda(), org, 30.0)
+    # pcl::PointXYZ layout: x, y, z, padding (16-byte stride)
+    padded = np.zeros((len(pts), 4), np.float32)
+    padded[:, :3] = pts
+    m2 = gpu.ProbabilisticMap(0.1)
+    m2.insert_point_cloud(padded, org, 30.0, stride=16)
+    o = port.pmap(0.1)
+    o.insert(pts, org, 30.0)
+    assert_same_map(m1, o)
+    assert_same_map(m2, o)
+
+
+def test_double_points(gpu, port):
+    rng = np.random.default_rng(3)
+    org = np.array([0.013, -0.27, 0.5])
+    pts = org + rng.normal(0, 3.0, (20000, 3))
+    m = gpu.ProbabilisticMap(0.05)
+    o = port.pmap(0.05)
+    for _ in range(4):
+        assert m.insert_point_cloud(pts, org, 4.0) == o.insert(pts, org, 4.0)
+    assert_same_map(m, o)
+
+
+def test_custom_options_and_clamps(gpu, port):
+    rng = np.random.default_rng(4)
+    opts = [-900000, 1300000, -2500000, 2000000, 100000]
+    m = gpu.ProbabilisticMap(0.1)
+    o = port.pmap(0.1)
+    m.options = opts
+    o.options = opts
+    assert list(m.options) == opts
+    org = np.zeros(3, np.float32)
+    for k in range(6):
+        pts = rng.normal(0, 1.5, (6000, 3)).astype(np.float32)
+        assert m.insert_point_cloud(pts, org, 2.0) == o.insert(pts, org, 2.0)
+    assert_same_map(m, o)
+    q = rng.integers(-40, 40, (50000, 3)).astype(np.int32)
+    assert np.array_equal(m.is_occupied(q), o.query(q)[0])
+    assert np.array_equal(m.is_free(q), o.query(q)[2])
+
+
+def test_edge_cases(gpu, port):
+    m = gpu.ProbabilisticMap(0.1)
+    o = port.pmap(0.1)
+    org = np.array([0.05, 0.05, 0.05], np.float32)
+    empty = np.zeros((0, 3), np.float32)
+    assert m.insert_point_cloud(empty, org, 5.0) == o.insert(empty, org, 5.0) == 0
+    assert m.update_count == o.update_count == 2
+    # points in the origin cell: no ray; duplicates; a point exactly at max range
+    pts = np.array([[0.06, 0.07, 0.08], [0.06, 0.07, 0.08], [5.05, 0.05, 0.05],
+                    [0.05, 5.05, 0.05], [-3.0, 2.0, 1.0]], np.float32)
+    for _ in range(4):
+        assert m.insert_point_cloud(pts, org, 5.0) == o.insert(pts, org, 5.0)
+    assert_same_map(m, o)
+
+
+def test_nonfinite_points_are_dropped(gpu, port):
+    rng = np.random.default_rng(5)
+    pts = rng.normal(0, 2, (5000, 3)).astype(np.float32)
+    bad = pts.copy()
+    bad[::17, 1] = np.nan
+    bad[::23, 2] = np.inf
+    keep = np.isfinite(bad).all(1)
+    m = gpu.ProbabilisticMap(0.1)
+    o = port.pmap(0.1)
+    org = np.zeros(3, np.float32)
+    m.insert_point_cloud(bad, org, 3.0)
+    o.insert(bad[keep], org, 3.0)
+    assert_same_map(m, o)
+
+
+def test_full_size_lidar_20_scans(gpu, port):
+    """The 64 x 2048 LiDAR workload at full size, all 20 scans, bit-exact."""
+    scene = synth.LidarScene()
+    m = gpu.ProbabilisticMap(scene.resolution)
+    o = port.pmap(scene.resolution)
+    total = 0
+    for k in range(20):
+        pts, org = scene.scan(k)
+        v = m.insert_point_cloud(pts, org, scene.max_range)
+        assert v == o.insert(pts, org, scene.max_range)
+        total += v
+    assert_same_map(m, o)
+    assert total > 20 * 131072
+
+
+def test_growth_from_tiny_pools(gpu, port):
+    cfg = gpu.Config(initial_leaves=16, initial_inners=4, hash_buckets=16)
+    scene = synth.LidarScene()
+    m = gpu.ProbabilisticMap(0.1, cfg)
+    o = port.pmap(0.1)
+    for k in range(3):
+        pts, org = scene.scan(k, n_points=30000)
+        assert m.insert_point_cloud(pts, org, 30.0) == o.insert(pts, org, 30.0)
+    assert_same_map(m, o)
+
+
+def test_pool_budget_exhaustion_reports_and_recovers(gpu):
+    cfg = gpu.Config(initial_leaves=16, initial_inners=4, hash_buckets=16,
+                     pool_budget_bytes=1 << 20)
+    scene = synth.LidarScene()
+    m = gpu.ProbabilisticMap(0.1, cfg)
+    pts, org = scene.scan(0, n_points=30000)
+    with pytest.raises(gpu.BonxaiError) as ei:
+        m.insert_point_cloud(pts, org, 30.0)
+    assert ei.value.status in (2, 3)
+    # the handle stays usable
+    q = np.zeros((10, 3), np.int32)
+    m.is_occupied(q)
+    m.clear()
+    small = np.array([[0.5, 0.5, 0.5]], np.float32)
+    m.insert_point_cloud(small, np.zeros(3, np.float32), 30.0)
+
+
+def test_kernel_timing_and_stats(gpu, port):
+    scene = synth.LidarScene()
+    m = gpu.ProbabilisticMap(0.1, gpu.Config(flags=gpu.FLAG_TIMING))
+    pts, org = scene.scan(0, n_points=20000)
+    v = m.insert_point_cloud(pts, org, 30.0)
+    st = m.last_stats()
+    assert st["points"] == 20000 and st["ray_cells_visited"] == v - 20000
+    t = m.kernel_times()
+    assert all(x >= 0 for x in t) and t[3] > 0
