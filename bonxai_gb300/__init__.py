@@ -110,6 +110,9 @@ _SIGS = {
     "bxg_pmap_last_stats": (_int, [_vp, _vp]),
     "bxg_pmap_kernel_times": (_int, [_vp, _vp]),
     "bxg_pmap_stream": (_vp, [_vp]),
+    "bxg_pmap_grid": (_vp, [_vp]),
+    "bxg_pmap_add_points": (_int, [_vp, _vp, _vp, _sz]),
+    "bxg_grid_store_if_on": (_int, [_vp, _vp, _vp, _sz]),
     "bxg_compute_rays": (_int, [_vp, _vp, _sz, _vp, _vp, _vp]),
 }
 
@@ -270,6 +273,11 @@ class VoxelGrid(_Handle):
         self._check(self.lib.bxg_grid_set_cells_off(self.h, p, n, _ptr(was)))
         return was
 
+    def store_if_on(self, coords, values):
+        p, keep, n = _in(coords, np.int32, 3)
+        v, keepv, _ = _in(values, self.dtype)
+        self._check(self.lib.bxg_grid_store_if_on(self.h, p, v, n))
+
     def is_cell_on(self, coords):
         p, keep, n = _in(coords, np.int32, 3)
         out = np.zeros(n, np.uint8)
@@ -392,6 +400,12 @@ class ProbabilisticMap(_Handle):
     def add_miss_points(self, points):
         p, keep, n = _in(points, np.float64, 3)
         self._check(self.lib.bxg_pmap_add_miss_points(self.h, p, n))
+
+    def add_points(self, points, kinds):
+        """Ordered mix of addHitPoint (kind 0) and addMissPoint (kind 1) calls."""
+        p, keep, n = _in(points, np.float64, 3)
+        k, keepk, _ = _in(kinds, np.uint8)
+        self._check(self.lib.bxg_pmap_add_points(self.h, p, k, n))
 
     addHitPoint = add_hit_points
     addMissPoint = add_miss_points

@@ -214,6 +214,21 @@ __global__ void k_get_values(DMap M, const int32_t* __restrict__ xyz, uint32_t n
   }
 }
 
+// Write-back of a mutable visitor: only cells that are on take the value.
+template <int ESZ>
+__global__ void k_store_if_on(DMap M, const int32_t* __restrict__ xyz,
+                              const uint8_t* __restrict__ vals, uint32_t n) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int x = xyz[3 * i], y = xyz[3 * i + 1], z = xyz[3 * i + 2];
+  const uint32_t lf = leaf_of(M, x, y, z, false);
+  if (lf == kNone) return;
+  const uint32_t ci = leaf_index(M, x, y, z);
+  if (!cell_is_on(M, lf, ci)) return;
+  copy_val<ESZ>(M.ldata + (static_cast<size_t>(lf) * M.lsize + ci) * ESZ,
+                vals + static_cast<size_t>(i) * ESZ);
+}
+
 // releaseUnusedMemory (bonxai.hpp:367-387): leaves whose mask is all off are
 // unlinked from their inner node and pushed on the free stack.
 __global__ void k_release_leaves(DMap M, uint32_t n_leaves) {
@@ -492,6 +507,31 @@ int bxg_grid_get_values(bxg_grid g, const int32_t* xyz, size_t n, void* out_valu
   }
   BXG_CUDA(m, cudaStreamSynchronize(m->stream));
   return BXG_OK;
+}
+
+int bxg_grid_store_if_on(bxg_grid g, const int32_t* xyz, const void* values, size_t n) {
+  if (check_grid(g)) return BXG_ERR_INVALID_ARG;
+  MapCore* m = &g->core;
+  if (!n || !m->dm.esz) return BXG_OK;
+  if (!xyz || !values || n >= 0x7FFFFFFFu) return set_error(m, BXG_ERR_INVALID_ARG, "null input");
+  cudaSetDevice(m->device);
+  const void* dxyz = nullptr;
+  const void* dvals = nullptr;
+  int st = stage_in(m, m->s_in, xyz, n * 12, &dxyz);
+  if (st) return st;
+  st = stage_in(m, m->s_in2, values, n * size_t(m->dm.esz), &dvals);
+  if (st) return st;
+  const unsigned blocks = unsigned((n + 255) / 256);
+  const int32_t* c = static_cast<const int32_t*>(dxyz);
+  const uint8_t* v = static_cast<const uint8_t*>(dvals);
+  switch (m->dm.esz) {
+    case 1: k_store_if_on<1><<<blocks, 256, 0, m->stream>>>(m->dm, c, v, uint32_t(n)); break;
+    case 2: k_store_if_on<2><<<blocks, 256, 0, m->stream>>>(m->dm, c, v, uint32_t(n)); break;
+    case 4: k_store_if_on<4><<<blocks, 256, 0, m->stream>>>(m->dm, c, v, uint32_t(n)); break;
+    default: k_store_if_on<8><<<blocks, 256, 0, m->stream>>>(m->dm, c, v, uint32_t(n)); break;
+  }
+  BXG_LAUNCHED(m);
+  return core_sync(m);
 }
 
 int bxg_grid_is_cell_on(bxg_grid g, const int32_t* xyz, size_t n, uint8_t* out) {

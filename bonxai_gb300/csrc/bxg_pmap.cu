@@ -135,12 +135,14 @@ __global__ void k_endpoints(DMap M, const uint8_t* __restrict__ pts, size_t stri
   dedup_min_insert(tab, tmask, cx, cy, cz, i, M);
 }
 
-// addHitPoint / addMissPoint batches: double points with a given kind.
+// addHitPoint / addMissPoint batches: double points with a given kind, or a
+// per-point kind (0 hit, 1 miss) when kinds != nullptr.
 __global__ void k_endpoints_kind(DMap M, const double* __restrict__ pts, uint32_t n, int kind,
-                                 double inv_res, int4* __restrict__ ep, uint4* tab,
-                                 uint32_t tmask) {
+                                 const uint8_t* __restrict__ kinds, double inv_res,
+                                 int4* __restrict__ ep, uint4* tab, uint32_t tmask) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
+  if (kinds) kind = kinds[i] ? EP_MISS : EP_HIT;
   const int cx = __double2int_rd(__dmul_rn(pts[3 * i + 0], inv_res));
   const int cy = __double2int_rd(__dmul_rn(pts[3 * i + 1], inv_res));
   const int cz = __double2int_rd(__dmul_rn(pts[3 * i + 2], inv_res));
@@ -591,7 +593,8 @@ int insert_impl(bxg_pmap m_, const PT* xyz, size_t stride, size_t n, const PT* o
   return finish_scan(pm, o[0], o[1], o[2], true, ray_cells, true);
 }
 
-int add_points(bxg_pmap m_, const double* xyz, size_t n, int kind) {
+int add_points(bxg_pmap m_, const double* xyz, size_t n, int kind,
+               const uint8_t* kinds = nullptr) {
   if (!m_) return BXG_ERR_INVALID_ARG;
   bxg_pmap_s* pm = m_;
   MapCore* m = &pm->core;
@@ -604,13 +607,18 @@ int add_points(bxg_pmap m_, const double* xyz, size_t n, int kind) {
     if (st) return st;
   }
   const void* dpts = nullptr;
+  const void* dkinds = nullptr;
   int st = stage_in(m, m->s_in, xyz, n * 24, &dpts);
   if (st) return st;
+  if (kinds) {
+    st = stage_in(m, m->s_in2, kinds, n, &dkinds);
+    if (st) return st;
+  }
   st = endpoint_phase(pm, uint32_t(n), 0, 0, 0,
                       [&](unsigned blocks, int4* ep, uint4* tab, uint32_t tmask) {
                         k_endpoints_kind<<<blocks, 256, 0, m->stream>>>(
                             m->dm, static_cast<const double*>(dpts), uint32_t(n), kind,
-                            m->inv_res, ep, tab, tmask);
+                            static_cast<const uint8_t*>(dkinds), m->inv_res, ep, tab, tmask);
                       });
   if (st) return st;
   // apply now so that queries see the endpoint updates, as in the reference
@@ -712,6 +720,17 @@ int bxg_pmap_add_hit_points(bxg_pmap m, const double* xyz, size_t n) {
 
 int bxg_pmap_add_miss_points(bxg_pmap m, const double* xyz, size_t n) {
   return add_points(m, xyz, n, EP_MISS);
+}
+
+int bxg_pmap_add_points(bxg_pmap m, const double* xyz, const uint8_t* kinds, size_t n) {
+  if (n && !kinds) return BXG_ERR_INVALID_ARG;
+  return add_points(m, xyz, n, EP_HIT, kinds);
+}
+
+bxg_grid bxg_pmap_grid(bxg_pmap m) {
+  // Both handle types hold their MapCore first and the grid entry points use
+  // only that, so the map itself serves as its VoxelGrid<CellT>.
+  return reinterpret_cast<bxg_grid>(m);
 }
 
 int bxg_pmap_update_free_cells(bxg_pmap pm, const double origin[3], uint64_t* ray_cells) {

@@ -118,6 +118,10 @@ int bxg_grid_set_cells_on(bxg_grid g, const int32_t* xyz, size_t n, const void* 
                           uint8_t* was_on);
 /* setCellOff(coord) (bonxai.hpp:556-569). */
 int bxg_grid_set_cells_off(bxg_grid g, const int32_t* xyz, size_t n, uint8_t* was_on);
+/* The write-back half of a mutable forEachCell visitor (bonxai.hpp:194-207):
+ * stores values[i] into cells that are on and leaves cells that are off (or
+ * missing) untouched. */
+int bxg_grid_store_if_on(bxg_grid g, const int32_t* xyz, const void* values, size_t n);
 /* ConstAccessor::isCellOn(coord) (bonxai.hpp:518-534). */
 int bxg_grid_is_cell_on(bxg_grid g, const int32_t* xyz, size_t n, uint8_t* out);
 
@@ -174,6 +178,10 @@ int bxg_pmap_insert_point_cloud_f32(bxg_pmap m, const float* xyz, size_t stride,
 int bxg_pmap_insert_point_cloud_f64(bxg_pmap m, const double* xyz, size_t stride, size_t n,
                                     const double origin[3], double max_range,
                                     uint64_t* ray_cells);
+/* A mixed, ordered batch of addHitPoint (kinds[i] = 0) and addMissPoint
+ * (kinds[i] = 1) calls: the lowest index among the points of one cell decides,
+ * exactly as the calls in this order would (probabilistic_map.cpp:30-54). */
+int bxg_pmap_add_points(bxg_pmap m, const double* xyz, const uint8_t* kinds, size_t n);
 /* Same, asynchronous on the handle's stream: returns after enqueueing. Errors
  * of the device phases are reported by the next synchronous call or by
  * bxg_pmap_synchronize. */
@@ -220,6 +228,10 @@ int bxg_pmap_last_stats(bxg_pmap m, uint64_t out[8]);
 int bxg_pmap_kernel_times(bxg_pmap m, float out[4]);
 /* The CUDA stream the handle runs on (a cudaStream_t). */
 void* bxg_pmap_stream(bxg_pmap m);
+/* grid() (probabilistic_map.hpp:70-72): a borrowed VoxelGrid<CellT> handle
+ * (value_bytes 4, the packed CellT word) over the map's own pools. Valid while
+ * the map lives; never pass it to bxg_grid_destroy. */
+bxg_grid bxg_pmap_grid(bxg_pmap m);
 
 /* ComputeRay(origin, end) (probabilistic_map.hpp:13-19,162-203) on the GPU for
  * n rays: out_len[i] = ray length; cells of ray i are written at

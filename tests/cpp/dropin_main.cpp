@@ -1,0 +1,144 @@
+// Caller code written against the reference's C++ API, compiled unchanged
+// against include/bonxai/bonxai.hpp and include/bonxai_map/probabilistic_map.hpp
+// (the GPU library). It follows the calls of the reference's
+// examples/tutorial.cpp and a LiDAR-style insertPointCloud loop, and writes
+// its results to text/binary files that tests/test_dropin_cpp.py compares with
+// the CPU oracle.
+//
+// usage: dropin_main <scans.bin> <out_dir>
+//   scans.bin: int32 n_scans, int32 n_points, float resolution, float max_range,
+//              then per scan: float origin[3], float xyz[n_points*3]
+#include <cstdio>
+#include <fstream>
+#include <iostream>
+#include <string>
+#include <vector>
+
+#include "bonxai/bonxai.hpp"
+#include "bonxai_map/probabilistic_map.hpp"
+
+struct PointXYZ {  // pcl::PointXYZ layout: x, y, z and padding
+  float x, y, z, pad;
+  PointXYZ() = default;
+  PointXYZ(float a, float b, float c) : x(a), y(b), z(c), pad(1.0f) {}
+};
+
+static int tutorial(const std::string& out) {
+  std::ofstream f(out);
+  const double VOXEL_RESOLUTION = 0.1;
+  Bonxai::VoxelGrid<long> grid(VOXEL_RESOLUTION);
+  Bonxai::BinaryVoxelGrid binaryGrid(VOXEL_RESOLUTION);
+  auto accessor = grid.createAccessor();
+  auto binaryAccessor = binaryGrid.createAccessor();
+  // the reference's tutorial fills this cube one scalar call at a time; the
+  // batch calls do the same writes in one pass each
+  std::vector<Bonxai::CoordT> coords;
+  std::vector<long> vals;
+  int count = 0;
+  for (double x = -1.0; x < 1.0; x += VOXEL_RESOLUTION) {
+    for (double y = -1.0; y < 1.0; y += VOXEL_RESOLUTION) {
+      for (double z = -1.0; z < 1.0; z += VOXEL_RESOLUTION) {
+        coords.push_back(grid.posToCoord(x, y, z));
+        vals.push_back(count++);
+      }
+    }
+  }
+  grid.setValues(coords, vals);
+  binaryGrid.setCellsOn(coords);
+  // a few scalar calls too
+  accessor.setValue(grid.posToCoord(0.55, 0.55, 0.55), 77);
+  binaryAccessor.setCellOn(grid.posToCoord(0.55, 0.55, 0.55));
+  f << "cells " << grid.activeCellsCount() << " " << binaryGrid.activeCellsCount() << "\n";
+
+  auto* origin_ptr = accessor.value(grid.posToCoord(0, 0, 0));
+  *origin_ptr = 500;
+  f << "origin " << *origin_ptr << "\n";
+  auto* far_voxel = accessor.value(grid.posToCoord(10, 10, 10), true);
+  (*far_voxel)++;
+  f << "far " << *far_voxel << "\n";
+
+  auto mutableVisitor = [&grid, &accessor](auto& value, const Bonxai::CoordT& coord) {
+    Bonxai::Point3D pos = grid.coordToPos(coord);
+    if (pos.z < -0.1) {
+      accessor.setCellOff(coord);
+    } else {
+      value = 1;
+    }
+  };
+  grid.forEachCell(mutableVisitor);
+
+  long sum = 0;
+  grid.forEachCell([&sum](const long& v, const Bonxai::CoordT&) { sum += v; });
+  f << "after_visit " << grid.activeCellsCount() << " sum " << sum << "\n";
+
+  auto constAccessor = grid.createConstAccessor();
+  const auto* cell = constAccessor.value(grid.posToCoord(0, 0, 0));
+  f << "const_origin " << (cell ? std::to_string(*cell) : std::string("nullptr")) << "\n";
+  cell = constAccessor.value(grid.posToCoord(0, 0, -0.2));
+  f << "const_below " << (cell ? std::to_string(*cell) : std::string("nullptr")) << "\n";
+  f << "binary_on " << binaryGrid.createConstAccessor().isCellOn(grid.posToCoord(0.55, 0.55, 0.55))
+    << "\n";
+  return 0;
+}
+
+static int lidar(const std::string& in, const std::string& outdir) {
+  std::ifstream f(in, std::ios::binary);
+  int32_t n_scans = 0, n_points = 0;
+  float res = 0, max_range = 0;
+  f.read(reinterpret_cast<char*>(&n_scans), 4);
+  f.read(reinterpret_cast<char*>(&n_points), 4);
+  f.read(reinterpret_cast<char*>(&res), 4);
+  f.read(reinterpret_cast<char*>(&max_range), 4);
+  Bonxai::ProbabilisticMap map(res);
+  std::vector<float> buf(size_t(n_points) * 3);
+  for (int s = 0; s < n_scans; s++) {
+    float o[3];
+    f.read(reinterpret_cast<char*>(o), 12);
+    f.read(reinterpret_cast<char*>(buf.data()), buf.size() * 4);
+    std::vector<PointXYZ> cloud;
+    cloud.reserve(n_points);
+    for (int i = 0; i < n_points; i++) cloud.emplace_back(buf[3 * i], buf[3 * i + 1], buf[3 * i + 2]);
+    map.insertPointCloud(cloud, PointXYZ(o[0], o[1], o[2]), max_range);
+  }
+  // hit and miss points by hand, then the free-space rays
+  for (int i = 0; i < 200; i++) {
+    const double a = 0.01 * i;
+    map.addHitPoint(Bonxai::Point3D{1.0 + a, -0.5 + 0.3 * a, 0.8});
+    if (i % 3 == 0) map.addMissPoint(Bonxai::Point3D{-2.0 - a, 0.5, 1.2 + 0.1 * a});
+  }
+  map.updateFreeCells(Bonxai::Point3D{0.05, 0.05, 1.0});
+
+  std::vector<Bonxai::CoordT> occ;
+  map.getOccupiedVoxels(occ);
+  std::ofstream fo(outdir + "/occupied.bin", std::ios::binary);
+  fo.write(reinterpret_cast<const char*>(occ.data()), occ.size() * sizeof(Bonxai::CoordT));
+
+  std::ofstream fc(outdir + "/cells.bin", std::ios::binary);
+  map.grid().forEachCell([&fc](const Bonxai::ProbabilisticMap::CellT& c, const Bonxai::CoordT& p) {
+    int32_t w;
+    std::memcpy(&w, &c, 4);
+    fc.write(reinterpret_cast<const char*>(&p), 12);
+    fc.write(reinterpret_cast<const char*>(&w), 4);
+  });
+  std::vector<Bonxai::CoordT> probe(occ.begin(), occ.begin() + std::min<size_t>(occ.size(), 50));
+  int n_occ = 0;
+  for (const auto& c : probe) n_occ += map.isOccupied(c);
+  std::ofstream ft(outdir + "/summary.txt");
+  ft << "occupied " << occ.size() << " probe_occ " << n_occ << " probe " << probe.size() << "\n";
+  return 0;
+}
+
+int main(int argc, char** argv) {
+  if (argc < 3) {
+    std::cerr << "usage: dropin_main <scans.bin> <out_dir>\n";
+    return 2;
+  }
+  try {
+    tutorial(std::string(argv[2]) + "/tutorial.txt");
+    lidar(argv[1], argv[2]);
+  } catch (const std::exception& e) {
+    std::cerr << "error: " << e.what() << "\n";
+    return 1;
+  }
+  return 0;
+}
