@@ -72,6 +72,7 @@ _SIGS = {
     "bxg_grid_destroy": (_int, [_vp]),
     "bxg_grid_pos_to_coord": (_int, [_vp, _vp, _sz, _vp]),
     "bxg_grid_set_values": (_int, [_vp, _vp, _vp, _sz, _vp]),
+    "bxg_grid_set_values_noalloc": (_int, [_vp, _vp, _vp, _sz]),
     "bxg_grid_set_values_at_points_f32": (_int, [_vp, _vp, _sz, _sz, _vp]),
     "bxg_grid_set_values_at_points_f64": (_int, [_vp, _vp, _sz, _sz, _vp]),
     "bxg_grid_get_values": (_int, [_vp, _vp, _sz, _vp, _vp, _int]),

@@ -11,6 +11,7 @@
 //      with atomicOr and writes the value.
 // Items are independent after step 1, so no two threads write one cell.
 #include <algorithm>
+#include <mutex>
 
 #include "bxg_internal.h"
 
@@ -705,3 +706,86 @@ int bxg_grid_synchronize(bxg_grid g) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// setValue batch that allocates nothing.
+//
+// For callers that must not allocate GPU memory while they run: a real-time
+// perception or control thread (cudaMalloc/cudaFree can block for
+// milliseconds and cudaFree synchronises the whole device), or a process that
+// reserves all of its device memory up front and forbids allocations later.
+// bxg_grid_set_values stages host inputs and grows its scratch table and the
+// node pools on demand, so it may call cudaMalloc; this variant never does.
+//
+// Its dedup table lives in the file-scope array below, which every GPU that
+// loads this library holds until the process exits. That caps one call at
+// kNoAllocMaxItems items; larger batches can be split, because consecutive
+// setValue batches give the same cells as one batch. The array is shared by
+// all calls on a device and keeps the last call's contents, so each call
+// first resets the part it uses; two calls that overlap on the GPU (different
+// streams or host threads at the same time) would race on it.
+// ---------------------------------------------------------------------------
+constexpr uint32_t kNoAllocMaxItems = 1u << 17;             // 131072 items per call
+constexpr uint32_t kNoAllocBuckets = 2u * kNoAllocMaxItems;  // 262144 x 16 B = 4 MiB
+
+static __device__ __align__(256) uint4 g_noalloc_dedup[kNoAllocBuckets];
+
+namespace {
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+uint4* g_noalloc_dev_ptr[kNoAllocMaxDevices] = {};
+
+// Device address of g_noalloc_dedup on the current device. In host code the
+// array's name only stands in for the symbol, so the address is looked up
+// once per device (with that device current) and cached.
+int noalloc_table(MapCore* m, uint4** out) {
+  if (m->device < 0 || m->device >= kNoAllocMaxDevices)
+    return set_error(m, BXG_ERR_INVALID_ARG, "device ordinal out of range for the no-alloc path");
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_dev_ptr[m->device]) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_dedup);
+    if (e != cudaSuccess) return cuda_fail(m, e, "cudaGetSymbolAddress(g_noalloc_dedup)");
+    g_noalloc_dev_ptr[m->device] = static_cast<uint4*>(p);
+  }
+  *out = g_noalloc_dev_ptr[m->device];
+  return BXG_OK;
+}
+}  // namespace
+
+extern "C" int bxg_grid_set_values_noalloc(bxg_grid g, const int32_t* d_xyz,
+                                           const void* d_values, size_t n) {
+  if (check_grid(g)) return BXG_ERR_INVALID_ARG;
+  MapCore* m = &g->core;
+  if (!n) return BXG_OK;
+  if (n > kNoAllocMaxItems)
+    return set_error(m, BXG_ERR_INVALID_ARG,
+                     "bxg_grid_set_values_noalloc takes at most 131072 items per call; "
+                     "split the batch");
+  if (!d_xyz || (m->dm.esz && !d_values))
+    return set_error(m, BXG_ERR_INVALID_ARG, "null input");
+  if (!is_device_ptr(d_xyz) || (m->dm.esz && !is_device_ptr(d_values)))
+    return set_error(m, BXG_ERR_INVALID_ARG,
+                     "bxg_grid_set_values_noalloc needs device-memory inputs");
+  cudaSetDevice(m->device);
+  uint4* tab = nullptr;
+  int st = noalloc_table(m, &tab);
+  if (st) return st;
+  const uint32_t cap = next_pow2(uint64_t(n) * 2);  // <= kNoAllocBuckets
+  BXG_CUDA(m, cudaMemsetAsync(tab, 0xFF, size_t(cap) * sizeof(uint4), m->stream));
+  const unsigned blocks = unsigned((n + 255) / 256);
+  const uint32_t nn = uint32_t(n);
+  k_dedup_insert<true><<<blocks, 256, 0, m->stream>>>(m->dm, d_xyz, nn, tab, cap - 1, nullptr);
+  BXG_LAUNCHED(m);
+  const uint8_t* vals = static_cast<const uint8_t*>(d_values);
+  switch (m->dm.esz) {
+    case 0: k_set_values<0><<<blocks, 256, 0, m->stream>>>(m->dm, d_xyz, vals, nn, tab, cap - 1); break;
+    case 1: k_set_values<1><<<blocks, 256, 0, m->stream>>>(m->dm, d_xyz, vals, nn, tab, cap - 1); break;
+    case 2: k_set_values<2><<<blocks, 256, 0, m->stream>>>(m->dm, d_xyz, vals, nn, tab, cap - 1); break;
+    case 4: k_set_values<4><<<blocks, 256, 0, m->stream>>>(m->dm, d_xyz, vals, nn, tab, cap - 1); break;
+    default: k_set_values<8><<<blocks, 256, 0, m->stream>>>(m->dm, d_xyz, vals, nn, tab, cap - 1); break;
+  }
+  BXG_LAUNCHED(m);
+  // Reports OUT_OF_POOL when the pools were full; they are not grown here.
+  return core_sync(m);
+}

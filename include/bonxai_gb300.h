@@ -100,6 +100,20 @@ int bxg_grid_pos_to_coord(bxg_grid g, const double* xyz, size_t n, int32_t* out_
  * state before that call. */
 int bxg_grid_set_values(bxg_grid g, const int32_t* xyz, const void* values, size_t n,
                         uint8_t* was_on);
+/* setValue batch that allocates no GPU memory (this entry point has no
+ * counterpart in the reference). For callers that cannot call cudaMalloc while
+ * they run -- a real-time thread, where an allocation can block for
+ * milliseconds and a free synchronises the device, or a process that reserves
+ * its device memory up front. Inputs must be device memory; at most 131072
+ * items per call (split larger batches: consecutive batches give the same
+ * cells); the grid's node pools are not grown, so a full pool returns
+ * BXG_ERR_OUT_OF_POOL (bxg_grid_set_values, or a larger initial_leaves, makes
+ * room). Its scratch table is a fixed 4 MiB array that each GPU loading this
+ * library holds until exit and that all calls share: calls that overlap on the
+ * GPU race. The first call on each device looks up that array's device
+ * address; make it before any stream capture. */
+int bxg_grid_set_values_noalloc(bxg_grid g, const int32_t* d_xyz, const void* d_values,
+                                size_t n);
 /* setValue(posToCoord(p), value) with float/double points (stride in bytes, 0 =
  * packed); the grid computes posToCoord in double. */
 int bxg_grid_set_values_at_points_f32(bxg_grid g, const float* xyz, size_t stride, size_t n,

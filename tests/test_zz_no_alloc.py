@@ -1,0 +1,69 @@
+"""The setValue batch that allocates no GPU memory.
+
+Some callers of this library must not allocate device memory while they run:
+a real-time mapping or control thread, where cudaMalloc can block for
+milliseconds and cudaFree synchronises the whole device, or a process that
+reserves its device memory up front. bxg_grid_set_values_noalloc serves them
+with a fixed scratch array instead of the growable scratch of
+bxg_grid_set_values. These tests call both through the C ABI on the same
+device-resident inputs, twice in a row (so the second call runs on a scratch
+array that still holds the first call's contents), and require identical grids.
+
+This file is collected last so that a run stopping at the first failure has
+already run every other test; it also passes alone in a fresh process.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+def _noalloc(lib, grid, d_xyz, d_vals):
+    return lib.bxg_grid_set_values_noalloc(grid.h, C.c_void_p(d_xyz.data_ptr()),
+                                           C.c_void_p(d_vals.data_ptr()), d_xyz.shape[0])
+
+
+def _batch(rng, n):
+    coords = rng.integers(-120, 120, (n, 3)).astype(np.int32)
+    coords[::7] = coords[1::7][: len(coords[::7])]  # repeated cells: last writer wins
+    vals = rng.random(n).astype(np.float32)
+    return coords, vals
+
+
+def test_noalloc_matches_set_values_on_two_calls(gpu):
+    lib = gpu.load_library()
+    rng = np.random.default_rng(2024)
+    cfg = gpu.Config(initial_leaves=1 << 15, initial_inners=1 << 10)
+    ref = gpu.VoxelGrid(0.05, dtype=np.float32, config=cfg)
+    cand = gpu.VoxelGrid(0.05, dtype=np.float32, config=cfg)
+    for _ in range(2):
+        coords, vals = _batch(rng, 100_000)
+        d_xyz = torch.from_numpy(coords).cuda()
+        d_vals = torch.from_numpy(vals).cuda()
+        assert lib.bxg_grid_set_values(ref.h, C.c_void_p(d_xyz.data_ptr()),
+                                       C.c_void_p(d_vals.data_ptr()), len(coords), None) == 0
+        st = _noalloc(lib, cand, d_xyz, d_vals)
+        assert st == 0, lib.bxg_last_error(cand.h)
+        a, av = ref.dump()
+        b, bv = cand.dump()
+        # bit-exact, the tolerance of every parity test here
+        assert np.array_equal(a, b)
+        assert np.array_equal(av.view(np.uint32), bv.view(np.uint32))
+
+
+def test_noalloc_rejects_oversized_and_host_inputs(gpu):
+    lib = gpu.load_library()
+    g = gpu.VoxelGrid(0.05, dtype=np.float32)
+    big = torch.zeros((131073, 3), dtype=torch.int32, device="cuda")
+    bigv = torch.zeros(131073, dtype=torch.float32, device="cuda")
+    assert _noalloc(lib, g, big, bigv) == 1
+    assert b"131072" in lib.bxg_last_error(g.h)
+    host_xyz = np.zeros((10, 3), np.int32)
+    host_val = np.zeros(10, np.float32)
+    st = lib.bxg_grid_set_values_noalloc(g.h, host_xyz.ctypes.data_as(C.c_void_p),
+                                         host_val.ctypes.data_as(C.c_void_p), 10)
+    assert st == 1 and b"device" in lib.bxg_last_error(g.h)
+    assert g.active_cells_count() == 0
