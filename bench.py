@@ -222,6 +222,7 @@ def run_ours(args):
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device=dev)
 
     cfg = bx.Config(flags=bx.FLAG_TIMING, rays_per_warp=args.rays_per_warp,
+                    ray_unroll=args.ray_unroll,
                     initial_leaves=1 << 19, initial_inners=1 << 15, hash_buckets=1 << 15)
     m = bx.ProbabilisticMap(scene.resolution, cfg)
     mr = scene.max_range
@@ -339,7 +340,7 @@ def run_ours(args):
         "ms_per_step": dev_ms_all / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "int32", "data": "synthetic",
         "config": dict(workload_config(scene), parallelism=f"replicas x{ws}",
-                       rays_per_warp=args.rays_per_warp),
+                       rays_per_warp=args.rays_per_warp, ray_unroll=args.ray_unroll),
         "roofline": roofline, "cpu_baseline": cpu,
         "e2e": None if args.no_e2e else {"value": e2e, "unit": "ray-cell updates/s",
                 "h2d_bytes_per_step": 131072 * 12, "d2h_bytes_per_step": 128,
@@ -355,13 +356,237 @@ def run_ours(args):
     return 0
 
 
+# ----------------------------------------------------------------------------
+# multi-map workload: 64 maps per tick, batched vs plain per-scan path
+# ----------------------------------------------------------------------------
+MM_RANGE = 10.0
+
+
+def multimap_inputs(n_maps: int):
+    """Base scan per map (log-uniform 10k..500k points, room or LiDAR
+    generator, resolution cycling 0.02/0.05/0.1 m). Tick t moves a LiDAR
+    sensor 0.5 m along +x (five poses, cycling) and re-observes a room from
+    its centre."""
+    from bonxai_gb300 import synth
+    specs = synth.multi_map_specs(n_maps)
+    base = []
+    for sp in specs:
+        if sp.kind == "lidar":
+            n_az = max(16, -(-sp.n_points // 64))
+            scene = synth.LidarScene(seed=sp.seed, n_az=n_az, max_range=MM_RANGE)
+            pts, o = scene.scan(0, n_points=sp.n_points)
+        else:
+            pts = synth.room_cloud(sp.n_points, seed=sp.seed)
+            o = ((synth.ROOM_LO + synth.ROOM_HI) / 2).astype(np.float32)
+        base.append((pts, o))
+    return specs, base
+
+
+def multimap_tick(specs, base, t):
+    scans = []
+    for sp, (pts, o) in zip(specs, base):
+        if sp.kind == "lidar":
+            d = np.array([0.5 * (t % 5), 0.0, 0.0], np.float32)
+            scans.append((pts + d, o + d))
+        else:
+            scans.append((pts, o))
+    return scans
+
+
+def run_multimap(args):
+    import torch
+    import bonxai_gb300 as bx
+
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    n_maps = args.maps
+    t0 = time.perf_counter()
+    specs, base = multimap_inputs(n_maps)
+    log(f"generated {n_maps} base scans in {time.perf_counter() - t0:.1f} s, "
+        f"{sum(len(b[0]) for b in base)} points per tick")
+    ticks = args.warmup + args.steps
+    big = bx.Config(initial_leaves=1 << 16, initial_inners=1 << 12, hash_buckets=1 << 14)
+    bmaps = [bx.ProbabilisticMap(sp.resolution, big) for sp in specs]
+    pmaps = [bx.ProbabilisticMap(sp.resolution, big) for sp in specs]
+    batch = bx.Batch(bx.Config(rays_per_warp=args.rays_per_warp, ray_unroll=args.ray_unroll))
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device=dev)
+
+    t_b, t_p, dev_b, V_b, V_p = 0.0, 0.0, 0.0, 0, 0
+    lat = []
+    phases = {}
+    for t in range(ticks):
+        scans = multimap_tick(specs, base, t)
+        pts = torch.from_numpy(np.concatenate([s[0] for s in scans])).to(dev)
+        off = np.concatenate([[0], np.cumsum([len(s[0]) for s in scans])]).astype(np.uint64)
+        org = np.stack([s[1] for s in scans])
+        dev_scans = [pts[int(off[i]):int(off[i + 1])] for i in range(n_maps)]
+        timed = t >= args.warmup
+        # batched tick
+        flush.fill_(t)
+        torch.cuda.synchronize()
+        a = time.perf_counter()
+        rc = batch.insert(bmaps, pts, off, org, MM_RANGE)
+        dt = time.perf_counter() - a
+        if timed:
+            t_b += dt
+            bst = batch.stats()
+            dev_b += bst["device_ms"] / 1e3
+            for k, v in bst["phase_ms"].items():
+                phases[k] = phases.get(k, 0.0) + v / args.steps
+            V_b += int(rc.sum())
+            lat.append(dt * 1e3)
+        # plain per-scan path, same inputs
+        flush.fill_(t)
+        torch.cuda.synchronize()
+        a = time.perf_counter()
+        vp = 0
+        for i in range(n_maps):
+            vp += pmaps[i].insert_point_cloud(dev_scans[i], org[i], MM_RANGE)
+        dt = time.perf_counter() - a
+        if timed:
+            t_p += dt
+            V_p += vp
+        if rc.sum() != vp:
+            raise SystemExit(f"tick {t}: batched {int(rc.sum())} != plain {vp} ray cells")
+    # bit-exact check of every map after the run
+    same = all(np.array_equal(bmaps[i].dump()[1], pmaps[i].dump()[1]) for i in range(n_maps))
+    value = V_b / t_b
+    plain = V_p / t_p
+    lat.sort()
+    line = {
+        "metric": "ray-cell updates/s (64-map batched tick)", "value": value,
+        "unit": "ray-cell updates/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * t_b / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+        "config": {"workload": "multimap_64", "maps": n_maps,
+                   "points_per_tick": int(off[-1]), "max_range_m": MM_RANGE,
+                   "resolutions_m": [0.02, 0.05, 0.1], "sizes": "log-uniform 10k..500k",
+                   "rays_per_warp": args.rays_per_warp, "ray_unroll": args.ray_unroll,
+                   "graph": batch.stats()["graph"],
+                   "l2": "flushed before every timed tick (256 MiB write)"},
+        "plain_per_scan_value": plain, "batched_over_plain": value / plain,
+        "batched_device_value": V_b / dev_b,
+        "tick_ms_p50": lat[len(lat) // 2], "tick_ms_p99": lat[min(len(lat) - 1, int(0.99 * len(lat)))],
+        "maps_bit_identical_batched_vs_plain": same,
+        "tick_phase_ms": phases,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ----------------------------------------------------------------------------
+# serving workload: 32 clients, Poisson arrivals, mixed requests
+# ----------------------------------------------------------------------------
+def run_serve(args):
+    import threading
+    import bonxai_gb300 as bx
+    from bonxai_gb300 import synth
+
+    n_clients = args.clients
+    rate = args.rate
+    duration = args.duration
+    rng0 = np.random.default_rng(5000)
+    # request payloads: slices of a few large base scans, shifted per client
+    t0 = time.perf_counter()
+    lidar = synth.LidarScene(seed=5001, n_az=4800, max_range=MM_RANGE)  # 307,200 rays
+    lid_pts, lid_o = lidar.scan(0, n_points=300_000)
+    room_pts = synth.room_cloud(300_000, seed=5002)
+    room_o = ((synth.ROOM_LO + synth.ROOM_HI) / 2).astype(np.float32)
+    coords_pool = rng0.integers([-100, -100, -20], [100, 100, 60], (1_000_000, 3)).astype(np.int32)
+    log(f"serving inputs ready in {time.perf_counter() - t0:.1f} s")
+    res = [0.1 if c % 2 == 0 else 0.05 for c in range(n_clients)]
+    cfg = bx.ServerConfig(pool_budget_bytes=args.budget_gb << 30, rays_per_warp=args.rays_per_warp,
+                          ray_unroll=args.ray_unroll, initial_leaves=1 << 14)
+    srv = bx.Server(res, cfg)
+
+    def client_stream(cid, rng, t_end, counts):
+        shift = np.array([0.7 * cid, -0.3 * cid, 0.0], np.float32)
+        t = time.perf_counter()
+        k = 0
+        while True:
+            t += rng.exponential(n_clients / rate)
+            if t > t_end:
+                return
+            d = t - time.perf_counter()
+            if d > 0:
+                time.sleep(d)
+            u = rng.random()
+            if u < 0.70:
+                n = int(np.exp(rng.uniform(np.log(10_000), np.log(300_000))))
+                if cid % 2 == 0:
+                    pts, o = lid_pts[:n] + shift, lid_o + shift
+                else:
+                    pts, o = room_pts[:n], room_o
+                srv.insert(cid, pts, o, MM_RANGE, discard=True)
+                counts[0] += 1
+            elif u < 0.95:
+                n = int(np.exp(rng.uniform(np.log(1_000), np.log(1_000_000))))
+                srv.query(cid, coords_pool[:n], mode=0, discard=True)
+                counts[1] += 1
+            else:
+                srv.get_occupied(cid, discard=True)
+                counts[2] += 1
+            k += 1
+
+    # warm-up: one insert per client
+    for cid in range(n_clients):
+        srv.insert(cid, lid_pts[:20000] if cid % 2 == 0 else room_pts[:20000],
+                   lid_o if cid % 2 == 0 else room_o, MM_RANGE, discard=True)
+    srv.drain()
+    base = srv.stats()
+    t_start = time.perf_counter()
+    t_end = t_start + duration
+    counts = [[0, 0, 0] for _ in range(n_clients)]
+    threads = [threading.Thread(target=client_stream,
+                                args=(c, np.random.default_rng(5100 + c), t_end, counts[c]))
+               for c in range(n_clients)]
+    for th in threads:
+        th.start()
+    for th in threads:
+        th.join()
+    srv.drain(600)
+    wall = time.perf_counter() - t_start
+    st = srv.stats()
+    done = st["completed"] - base["completed"]
+    line = {
+        "metric": "served requests/s (32-client mixed stream)", "value": done / wall,
+        "unit": "requests/s", "n_gpus": 1, "steps": int(done), "warmup": n_clients,
+        "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "int32", "data": "synthetic",
+        "config": {"workload": "serve_32", "clients": n_clients, "offered_rate_rps": rate,
+                   "duration_s": duration, "mix": "70% insert 10k-300k pts, 25% isOccupied "
+                   "1k-1M coords, 5% getOccupiedVoxels", "budget_gb": args.budget_gb,
+                   "resolutions_m": [0.1, 0.05], "max_range_m": MM_RANGE},
+        "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"],
+        "insert_p50_ms": st["insert_p50_ms"], "insert_p99_ms": st["insert_p99_ms"],
+        "lookup_p50_ms": st["lookup_p50_ms"], "lookup_p99_ms": st["lookup_p99_ms"],
+        "occupied_p50_ms": st["occupied_p50_ms"], "occupied_p99_ms": st["occupied_p99_ms"],
+        "ray_cell_updates_per_s": (st["ray_cells"] - base["ray_cells"]) / wall,
+        "lookups_per_s": (st["lookup_coords"] - base["lookup_coords"]) / wall,
+        "ticks": st["ticks"] - base["ticks"], "rejected": st["rejected"],
+        "gpu_busy_frac": (st["busy_s"] - base["busy_s"]) / wall,
+        "submitted": [sum(c[i] for c in counts) for i in range(3)],
+        "pool_bytes": st["pool_bytes"],
+    }
+    srv.close()
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="lidar", choices=["lidar", "multimap", "serve"])
+    ap.add_argument("--maps", type=int, default=64)
+    ap.add_argument("--clients", type=int, default=32)
+    ap.add_argument("--rate", type=float, default=2000.0, help="offered requests/s (serve)")
+    ap.add_argument("--duration", type=float, default=20.0, help="seconds of load (serve)")
+    ap.add_argument("--budget-gb", type=int, default=40)
     ap.add_argument("--rays-per-warp", type=int, default=1)
+    ap.add_argument("--ray-unroll", type=int, default=1)
     ap.add_argument("--cpu-scans", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true",
@@ -372,6 +597,10 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "multimap":
+        return run_multimap(args)
+    if args.workload == "serve":
+        return run_serve(args)
     return run_ours(args)
 
 

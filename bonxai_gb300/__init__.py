@@ -19,7 +19,8 @@ from pathlib import Path
 
 import numpy as np
 
-__all__ = ["VoxelGrid", "ProbabilisticMap", "BonxaiError", "Config", "load_library",
+__all__ = ["VoxelGrid", "ProbabilisticMap", "Batch", "Server", "BonxaiError", "Config",
+           "ServerConfig", "load_library",
            "compute_rays", "library_path", "CLEAR_MEMORY", "SET_ALL_CELLS_OFF"]
 
 PKG = Path(__file__).resolve().parent
@@ -30,6 +31,7 @@ SET_ALL_CELLS_OFF = 1
 
 FLAG_KEEP_NONFINITE = 1
 FLAG_TIMING = 2
+FLAG_NO_GRAPH = 4
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "node pool exhausted", 3: "root hash full",
           4: "device wait timed out", 5: "CUDA error", 6: "no CUDA device",
@@ -47,7 +49,8 @@ class Config(C.Structure):
                 ("initial_inners", C.c_uint32), ("hash_buckets", C.c_uint32),
                 ("hash_load_factor", C.c_float), ("device", C.c_int),
                 ("stream", C.c_void_p), ("rays_per_warp", C.c_uint32),
-                ("block_size", C.c_uint32), ("flags", C.c_uint32)]
+                ("block_size", C.c_uint32), ("flags", C.c_uint32),
+                ("ray_unroll", C.c_uint32)]
 
     def __init__(self, **kw):
         super().__init__()
@@ -115,6 +118,23 @@ _SIGS = {
     "bxg_pmap_add_points": (_int, [_vp, _vp, _vp, _sz]),
     "bxg_grid_store_if_on": (_int, [_vp, _vp, _vp, _sz]),
     "bxg_compute_rays": (_int, [_vp, _vp, _sz, _vp, _vp, _vp]),
+    "bxg_batch_create": (_int, [_vp, _vp]),
+    "bxg_batch_destroy": (_int, [_vp]),
+    "bxg_batch_last_error": (C.c_char_p, [_vp]),
+    "bxg_batch_insert_f32": (_int, [_vp, _vp, _sz, _vp, _vp, _vp, _vp, _vp]),
+    "bxg_batch_stats": (_int, [_vp, _vp]),
+    "bxg_batch_phase_ms": (_int, [_vp, _vp]),
+    "bxg_server_config_default": (None, [_vp]),
+    "bxg_server_create": (_int, [_vp, _vp, _sz, _vp]),
+    "bxg_server_destroy": (_int, [_vp]),
+    "bxg_server_last_error": (C.c_char_p, [_vp]),
+    "bxg_server_insert": (_int, [_vp, C.c_uint32, _vp, _sz, _vp, _dbl, _int, _vp]),
+    "bxg_server_query": (_int, [_vp, C.c_uint32, _vp, _sz, _int, _int, _vp]),
+    "bxg_server_get_occupied": (_int, [_vp, C.c_uint32, _int, _vp]),
+    "bxg_server_wait": (_int, [_vp, C.c_uint64, _dbl, _vp, _vp, _sz]),
+    "bxg_server_drain": (_int, [_vp, _dbl]),
+    "bxg_server_stats": (_int, [_vp, _vp]),
+    "bxg_server_map": (_vp, [_vp, C.c_uint32]),
 }
 
 _lib = None
@@ -503,6 +523,163 @@ class ProbabilisticMap(_Handle):
         out = (C.c_float * 4)()
         self._check(self.lib.bxg_pmap_kernel_times(self.h, out))
         return [float(x) for x in out]
+
+
+class Batch(_Handle):
+    """One insertPointCloud per map for many maps per call, in one persistent
+    graph-replayed launch (bxg_batch_insert_f32)."""
+    _destroy = "bxg_batch_destroy"
+
+    def __init__(self, config: Config | None = None):
+        self.lib = load_library()
+        h = C.c_void_p()
+        st = self.lib.bxg_batch_create(C.byref(h), C.byref(config) if config else None)
+        if st:
+            raise BonxaiError(st, "bxg_batch_create")
+        self.h = h
+
+    def _check(self, st: int):
+        if st != 0:
+            msg = self.lib.bxg_batch_last_error(self.h)
+            raise BonxaiError(st, msg.decode() if msg else "")
+
+    def insert(self, maps, points, offsets, origins, max_ranges):
+        """points: packed float32 [N,3] (numpy or CUDA tensor) holding every
+        scan back to back; offsets: N_scans+1 int64; returns ray cells per scan."""
+        n = len(maps)
+        handles = (C.c_void_p * n)(*[m.h.value for m in maps])
+        p, keep, _ = _in(points, np.float32, 3)
+        off = np.ascontiguousarray(offsets, np.uint64)
+        org = np.ascontiguousarray(np.asarray(origins, np.float32).reshape(n, 3))
+        mr = np.ascontiguousarray(np.broadcast_to(np.asarray(max_ranges, np.float64), (n,)))
+        out = np.zeros(n, np.uint64)
+        self._check(self.lib.bxg_batch_insert_f32(self.h, handles, n, p, _ptr(off), _ptr(org),
+                                                  _ptr(mr), _ptr(out)))
+        return out
+
+    def stats(self) -> dict:
+        out = (C.c_double * 8)()
+        self._check(self.lib.bxg_batch_stats(self.h, out))
+        ph = (C.c_double * 5)()
+        self._check(self.lib.bxg_batch_phase_ms(self.h, ph))
+        return {"device_ms": out[0], "graph": bool(out[1]), "retried_maps": int(out[2]),
+                "ticks": int(out[3]), "grid": int(out[4]), "launches": int(out[5]),
+                "phase_ms": {"clear": ph[0], "endpoints": ph[1], "winners": ph[2],
+                             "prefix": ph[3], "rays": ph[4]}}
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("pool_budget_bytes", C.c_size_t), ("max_scans_per_tick", C.c_uint32),
+                ("max_points_per_tick", C.c_uint64), ("max_lookups_per_tick", C.c_uint64),
+                ("device", C.c_int), ("rays_per_warp", C.c_uint32), ("ray_unroll", C.c_uint32),
+                ("flags", C.c_uint32), ("initial_leaves", C.c_uint32)]
+
+    def __init__(self, **kw):
+        super().__init__()
+        self.device = -1
+        for k, v in kw.items():
+            setattr(self, k, v)
+
+
+class ServerResult(C.Structure):
+    _fields_ = [("status", C.c_int), ("kind", C.c_int), ("map", C.c_uint32),
+                ("ray_cells", C.c_uint64), ("n_out", C.c_size_t), ("latency_ms", C.c_double),
+                ("queue_ms", C.c_double), ("tick", C.c_uint64)]
+
+
+class Server(_Handle):
+    """Continuous-batching server over one persistent map per client
+    (bxg_server_*). Requests on one map run in submission order."""
+    _destroy = "bxg_server_destroy"
+
+    def __init__(self, resolutions, config: ServerConfig | None = None):
+        self.lib = load_library()
+        res = np.ascontiguousarray(resolutions, np.float64)
+        h = C.c_void_p()
+        st = self.lib.bxg_server_create(C.byref(h), _ptr(res), len(res),
+                                        C.byref(config) if config else None)
+        if st:
+            raise BonxaiError(st, "bxg_server_create")
+        self.h = h
+        self.n_maps = len(res)
+
+    def _check(self, st: int):
+        if st != 0:
+            msg = self.lib.bxg_server_last_error(self.h)
+            raise BonxaiError(st, msg.decode() if msg else "")
+
+    def insert(self, map_id, points, origin, max_range, discard=False) -> int:
+        p, keep, n = _in(points, np.float32, 3)
+        o = np.ascontiguousarray(np.asarray(origin, np.float32).reshape(3))
+        t = C.c_uint64()
+        self._check(self.lib.bxg_server_insert(self.h, int(map_id), p, n, _ptr(o),
+                                               float(max_range), int(discard), C.byref(t)))
+        return t.value
+
+    def query(self, map_id, coords, mode=0, discard=False) -> int:
+        p, keep, n = _in(coords, np.int32, 3)
+        t = C.c_uint64()
+        self._check(self.lib.bxg_server_query(self.h, int(map_id), p, n, int(mode), int(discard),
+                                              C.byref(t)))
+        return t.value
+
+    def get_occupied(self, map_id, discard=False) -> int:
+        t = C.c_uint64()
+        self._check(self.lib.bxg_server_get_occupied(self.h, int(map_id), int(discard),
+                                                     C.byref(t)))
+        return t.value
+
+    def wait_query(self, ticket, n, timeout=120.0):
+        res = ServerResult()
+        out = np.zeros(max(n, 1), np.uint8)
+        self._check(self.lib.bxg_server_wait(self.h, int(ticket), float(timeout), C.byref(res),
+                                             _ptr(out), n))
+        return self._res(res), out[:res.n_out]
+
+    def wait_insert(self, ticket, timeout=120.0):
+        res = ServerResult()
+        self._check(self.lib.bxg_server_wait(self.h, int(ticket), float(timeout), C.byref(res),
+                                             None, 0))
+        return self._res(res)
+
+    def wait_occupied(self, ticket, timeout=120.0):
+        res = ServerResult()
+        self._check(self.lib.bxg_server_wait(self.h, int(ticket), float(timeout), C.byref(res),
+                                             None, 0))
+        n = res.n_out
+        out = np.zeros((max(n, 1), 3), np.int32)
+        self._check(self.lib.bxg_server_wait(self.h, int(ticket), float(timeout), C.byref(res),
+                                             _ptr(out), n))
+        o = out[:n]
+        return self._res(res), o[np.lexsort((o[:, 2], o[:, 1], o[:, 0]))]
+
+    @staticmethod
+    def _res(r):
+        return {"status": r.status, "kind": r.kind, "map": r.map, "ray_cells": int(r.ray_cells),
+                "n_out": int(r.n_out), "latency_ms": r.latency_ms, "queue_ms": r.queue_ms,
+                "tick": int(r.tick)}
+
+    def drain(self, timeout=600.0):
+        self._check(self.lib.bxg_server_drain(self.h, float(timeout)))
+
+    def stats(self) -> dict:
+        out = (C.c_double * 20)()
+        self._check(self.lib.bxg_server_stats(self.h, out))
+        keys = ["completed", "inserts", "lookups", "occupied", "ticks", "p50_ms", "p99_ms",
+                "insert_p50_ms", "insert_p99_ms", "lookup_p50_ms", "lookup_p99_ms", "ray_cells",
+                "lookup_coords", "rejected", "busy_s", "span_s", "occupied_p50_ms",
+                "occupied_p99_ms", "pool_bytes"]
+        return {k: out[i] for i, k in enumerate(keys)}
+
+    def map_dump(self, map_id):
+        """Cells of one client's map (after drain), sorted."""
+        h = self.lib.bxg_server_map(self.h, int(map_id))
+        m = ProbabilisticMap.__new__(ProbabilisticMap)
+        m.lib, m.h = self.lib, C.c_void_p(h)
+        try:
+            return m.dump()
+        finally:
+            m.h = None  # borrowed: the server owns it
 
 
 def compute_rays(origins, ends):

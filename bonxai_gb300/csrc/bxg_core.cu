@@ -300,6 +300,7 @@ int core_init(MapCore* m, double res, int ib, int lb, size_t esz, const bxg_conf
   m->load_factor = cfg.hash_load_factor > 0 ? cfg.hash_load_factor : 0.5f;
   m->rays_per_warp = cfg.rays_per_warp;
   m->block_size = cfg.block_size;
+  m->ray_unroll = cfg.ray_unroll;
   DMap& d = m->dm;
   d.ib = ib;
   d.lb = lb;
@@ -351,6 +352,7 @@ int core_sync(MapCore* m, uint32_t* err_bits_out) {
   BXG_CUDA(m, cudaStreamSynchronize(m->stream));
   const uint32_t err = m->h_ctr[C_ERR];
   if (err_bits_out) *err_bits_out = err;
+  m->dm.has_free = m->h_ctr[C_FREE_LEAF] > 0 ? 1u : 0u;
   bool fix = false;
   if (m->h_ctr[C_INNER] > m->dm.icap) {
     m->h_ctr[C_INNER] = m->dm.icap;
@@ -409,6 +411,28 @@ int core_maintain(MapCore* m) {
   if (inner > 0.75 * m->dm.icap) grow_inner(m, size_t(m->dm.icap) * 2);
   if (leaves > 0.75 * m->dm.lcap) grow_leaf(m, size_t(m->dm.lcap) * 2);
   m->err.clear();
+  return BXG_OK;
+}
+
+int core_reserve(MapCore* m, size_t leaves, size_t inners) {
+  const size_t lused = m->h_ctr[C_LEAF], lfree = m->h_ctr[C_FREE_LEAF];
+  const size_t lavail = (m->dm.lcap > lused ? m->dm.lcap - lused : 0) + lfree;
+  if (lavail < leaves) {
+    const int st = grow_leaf(m, std::max<size_t>(size_t(m->dm.lcap) * 2, lused + leaves));
+    if (st) return st;
+  }
+  const size_t iused = m->h_ctr[C_INNER];
+  if ((m->dm.icap > iused ? m->dm.icap - iused : 0) < inners) {
+    const int st = grow_inner(m, std::max<size_t>(size_t(m->dm.icap) * 2, iused + inners));
+    if (st) return st;
+  }
+  const size_t hcap = size_t(m->dm.hmask) + 1;
+  if (m->h_ctr[C_ROOTS] + inners > m->load_factor * hcap) {
+    size_t want = hcap * 2;
+    while (m->h_ctr[C_ROOTS] + inners > m->load_factor * want) want *= 2;
+    const int st = grow_hash(m, want);
+    if (st) return st;
+  }
   return BXG_OK;
 }
 

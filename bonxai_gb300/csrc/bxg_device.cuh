@@ -26,8 +26,8 @@
 //
 // Concurrency: creation is lock-free with bounded waits. A root is inserted by
 // a 128-bit compare-and-swap of the whole bucket; the thread that inserted it
-// allocates the inner slot and publishes it with a release store while other
-// threads that need it wait (bounded, with backoff). Leaves use the same
+// allocates the inner slot and publishes it while other threads that need it
+// wait (bounded, with backoff). Leaves use the same
 // protocol on the inner node's child word (kNone -> kPending -> slot). A wait
 // that runs out sets an error bit and returns kNone; no kernel waits forever.
 #pragma once
@@ -88,6 +88,7 @@ struct DMap {
   int4* lkey;
   uint32_t* lfree;  // stack of released leaf slots
   uint32_t lcap;
+  uint32_t has_free;  // host's view: the free stack may be non-empty
   // counters
   uint32_t* ctr;
 };
@@ -102,6 +103,12 @@ __device__ __forceinline__ uint32_t ld_acquire(const uint32_t* p) {
 }
 __device__ __forceinline__ void st_release(uint32_t* p, uint32_t v) {
   asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+// Publication of a freshly allocated slot. What a reader needs behind the slot
+// (the node's zeroed mask/cells, its kNone children) was written before the
+// kernel started, so no release ordering is needed -- only visibility.
+__device__ __forceinline__ void st_publish(uint32_t* p, uint32_t v) {
+  *reinterpret_cast<volatile uint32_t*>(p) = v;
 }
 __device__ __forceinline__ uint4 ld_volatile4(const uint4* p) {
   uint4 v;
@@ -197,9 +204,11 @@ __device__ __forceinline__ uint32_t alloc_inner(const DMap& M) {
   }
   return i;
 }
-// Released leaves are reused first (their masks and cells are all zero).
+// Released leaves are reused first (their masks and cells are all zero). The
+// free stack is only filled by releaseUnusedMemory, so kernels launched while
+// the host knows it is empty skip the probe.
 __device__ __forceinline__ uint32_t alloc_leaf(const DMap& M) {
-  if (ld_volatile(M.ctr + C_FREE_LEAF) > 0) {
+  if (M.has_free && ld_volatile(M.ctr + C_FREE_LEAF) > 0) {
     const int prev = static_cast<int>(atomicSub(M.ctr + C_FREE_LEAF, 1u));
     if (prev > 0) return M.lfree[prev - 1];
     atomicAdd(M.ctr + C_FREE_LEAF, 1u);  // lost the race for the last entry
@@ -233,12 +242,12 @@ static __device__ __noinline__ uint32_t root_value_wait(const DMap& M, uint4* b)
   uint32_t* wp = &b->w;
   unsigned ns = 32;
   for (int it = 0; it < kSpinLimit; ++it) {
-    const uint32_t w = ld_acquire(wp);
+    const uint32_t w = ld_volatile(wp);
     if (w < kPending) return w;
     if (w == kNone) {
       if (atomicCAS(wp, kNone, kPending) == kNone) {
         const uint32_t in = alloc_inner(M);
-        st_release(wp, in);
+        st_publish(wp, in);
         return in;
       }
       continue;
@@ -266,9 +275,9 @@ static __device__ __noinline__ uint32_t root_get_or_create(const DMap& M, int x,
                  make_uint4(static_cast<uint32_t>(x), static_cast<uint32_t>(y),
                             static_cast<uint32_t>(z), kPending));
       if (eq4(v, kEmpty)) {
-        atomicAdd(M.ctr + C_ROOTS, 1u);
         const uint32_t in = alloc_inner(M);
-        st_release(&b->w, in);
+        st_publish(&b->w, in);
+        atomicAdd(M.ctr + C_ROOTS, 1u);
         return in;
       }
       if (!key_eq(v, x, y, z)) continue;
@@ -278,6 +287,23 @@ static __device__ __noinline__ uint32_t root_get_or_create(const DMap& M, int x,
   }
   set_err(M, ERR_HASH_FULL);
   return kNone;
+}
+
+// Fast path of root_get_or_create for hot loops: up to four probes with plain
+// (L1-cacheable) loads. kPending means "take the slow path" -- the key is
+// missing, still being created, or the probe chain is long. A stale or torn
+// read can only look like one of those (a valid key never has an all-ones
+// component), so the slow path always settles it.
+__device__ __forceinline__ uint32_t root_probe_fast(const DMap& M, int x, int y, int z) {
+  uint32_t h = root_hash(M, x, y, z) & M.hmask;
+#pragma unroll 1
+  for (int p = 0; p < 4; ++p) {
+    const uint4 b = M.buckets[h];
+    if (key_eq(b, x, y, z)) return b.w < kPending ? b.w : kPending;
+    if (static_cast<int>(b.x) == kEmptyKey) return kPending;
+    h = (h + 1) & M.hmask;
+  }
+  return kPending;
 }
 
 // ---------------------------------------------------------------------------
@@ -294,12 +320,12 @@ static __device__ __noinline__ uint32_t leaf_get_or_create(const DMap& M, uint32
       const uint32_t old = atomicCAS(slot, kNone, kPending);
       if (old == kNone) {
         const uint32_t lf = alloc_leaf(M);
-        if (lf != kNone) {
+        st_publish(slot, lf);
+        if (lf != kNone) {  // read only by later kernels (iteration, release)
           M.lkey[lf] = make_int4(lx, ly, lz, static_cast<int>(in));
           atomicOr(M.imask + static_cast<size_t>(in) * M.iwords + (ii >> 6),
                    1ull << (ii & 63));
         }
-        st_release(slot, lf);
         return lf;
       }
       c = old;
@@ -307,7 +333,7 @@ static __device__ __noinline__ uint32_t leaf_get_or_create(const DMap& M, uint32
     }
     __nanosleep(ns);
     ns = ns < 1024 ? ns * 2 : 1024;
-    c = ld_acquire(slot);
+    c = ld_volatile(slot);
   }
   set_err(M, ERR_WAIT);
   return kNone;
@@ -340,6 +366,11 @@ __device__ __forceinline__ bool cell_is_on(const DMap& M, uint32_t lf, uint32_t 
 __device__ __forceinline__ bool cell_set_on(const DMap& M, uint32_t lf, uint32_t ci) {
   const unsigned long long bit = 1ull << (ci & 63);
   return (atomicOr(mask_word(M, lf, ci), bit) & bit) != 0ull;
+}
+// Turns a cell on without reading the mask first (the result is unused, so
+// this compiles to a fire-and-forget reduction).
+__device__ __forceinline__ void cell_or_on(const DMap& M, uint32_t lf, uint32_t ci) {
+  atomicOr(mask_word(M, lf, ci), 1ull << (ci & 63));
 }
 // Turns the cell on, skipping the atomic when a plain read already shows it on.
 __device__ __forceinline__ void cell_mark_on(const DMap& M, uint32_t lf, uint32_t ci) {

@@ -247,6 +247,7 @@ __global__ void k_release_leaves(DMap M, uint32_t n_leaves) {
   const uint32_t slot = atomicAdd(M.ctr + C_FREE_LEAF, 1u);
   M.lfree[slot] = lf;
 }
+// (the host sets has_free when it next reads the counters)
 
 // Roots whose inner node has no leaf left are removed. Removal from an
 // open-addressing table would break probe chains, so the surviving buckets

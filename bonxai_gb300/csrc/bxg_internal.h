@@ -73,7 +73,7 @@ struct MapCore {
   DMap dm{};
   size_t budget = 0;
   float load_factor = 0.5f;
-  uint32_t rays_per_warp = 0, block_size = 0;
+  uint32_t rays_per_warp = 0, block_size = 0, ray_unroll = 0;
 
   // pools
   DevBuf buckets, ichild, imask, lmask, ldata, lkey, lfree, ctr;
@@ -144,4 +144,32 @@ void launch_rehash(MapCore* m, const uint4* old_b, uint32_t old_cap, const DMap&
 void set_create_error(const std::string& msg);
 const MapCore* core_of_handle(const void* handle);
 
+}  // namespace bxg
+
+// A ProbabilisticMap handle: a map core plus the scan state of
+// probabilistic_map.hpp:127-134.
+struct bxg_pmap_s {
+  bxg::MapCore core;
+  bxg_pmap_options opt{};
+  int update_count = 1;      // _update_count (probabilistic_map.hpp:129)
+  uint64_t cast_ub = 0;      // upper bound of queued rays on the device
+  uint64_t last_stats[8] = {0};
+  float last_times[4] = {0};
+  uint32_t last_new_leaves = 0;  // leaves created by the last scan (pool headroom)
+  cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  ~bxg_pmap_s() {
+    for (auto& e : ev)
+      if (e) cudaEventDestroy(e);
+  }
+};
+
+namespace bxg {
+// Completes a scan whose endpoints were listed (and possibly applied) by a
+// batched tick but whose map ran out of pool: grows the pools and re-runs the
+// idempotent endpoint completion and ray phases on the map's own stream.
+int pmap_complete_scan(bxg_pmap_s* pm, const int4* d_cast, const uint32_t* d_count,
+                       uint32_t cap, int ox, int oy, int oz, int32_t u);
+// Grows the map's pools so that the next scan has at least `leaves` free leaf
+// slots and the root hash stays under its load factor.
+int core_reserve(MapCore* m, size_t leaves, size_t inners);
 }  // namespace bxg

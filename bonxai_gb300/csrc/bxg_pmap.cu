@@ -3,31 +3,16 @@
 // bonxai_map/include/bonxai_map/probabilistic_map.hpp and
 // bonxai_map/src/probabilistic_map.cpp.
 //
-// Why a scan parallelises without changing its result. Let u be the scan
-// counter (1, 2, 3, cycling; probabilistic_map.cpp:103-105).
-//  * Endpoint phase (insertPointCloud loop + addHit/MissPoint, hpp:146-158,
-//    cpp:30-54). Only endpoint cells change, and each changes at most once:
-//    the first point (lowest input index) that lands in a cell whose
-//    update_id != u updates it and queues one ray; every later point in that
-//    cell sees update_id == u and does nothing. A cell that already had
-//    update_id == u before the scan is neither updated nor ray-cast. So the
-//    outcome per cell depends only on its pre-scan word and the lowest index
-//    landing in it.
-//  * Ray phase (updateFreeCells, cpp:77-106). Every queued ray visits the
-//    origin cell and the next max-1 Bresenham cells; each visited cell is
-//    created (T{} = {0, 0}) and, if its update_id != u, becomes
-//    {max(p + miss, clamp_min), u}. After the endpoint phase the only writes
-//    are this one function of the word, so the order of rays and cells is
-//    irrelevant and racing writers store the same value: a plain load and a
-//    conditional store suffice.
+// Why a scan parallelises without changing its result: see bxg_scan.cuh.
 //
 // Kernels per scan (all on the handle's stream):
 //   k_endpoints   fp64 endpoint of each point, exactly as hpp:147-156 rounds
 //                 it; lowest index per endpoint cell via a scratch hash table.
 //   k_winners     the lowest-index point of each cell reads the pre-scan word;
-//                 unless update_id == u it appends {cell, hit/miss} to the ray
-//                 list (and counts the ray length for the ray-cell total).
-//   k_apply       each listed endpoint creates its cell and applies hit/miss.
+//                 unless update_id == u it applies its hit/miss and appends
+//                 {cell, hit/miss} to the ray list (and counts the ray length
+//                 for the ray-cell total).
+//   k_apply       only after a pool ran out: completes the listed endpoints.
 //   k_rays        lane-strided Bresenham over every listed ray: a group of W
 //                 lanes walks one ray, W consecutive cells per step, creating
 //                 leaves on the way and applying the miss update.
@@ -37,67 +22,11 @@
 #include <vector>
 
 #include "bxg_internal.h"
-
-struct bxg_pmap_s {
-  bxg::MapCore core;
-  bxg_pmap_options opt{};
-  int update_count = 1;           // _update_count (probabilistic_map.hpp:129)
-  uint64_t cast_ub = 0;           // upper bound of queued rays on the device
-  uint64_t last_stats[8] = {0};
-  float last_times[4] = {0};
-  cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
-  ~bxg_pmap_s() {
-    for (auto& e : ev)
-      if (e) cudaEventDestroy(e);
-  }
-};
+#include "bxg_scan.cuh"
 
 namespace bxg {
 
-struct Opts {
-  int32_t miss, hit, cmin, cmax;
-};
-
-// ---------------------------------------------------------------------------
-// endpoint phase
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ bool finite3(double a, double b, double c) {
-  return isfinite(a) && isfinite(b) && isfinite(c);
-}
-
-// Lowest index per endpoint cell (scratch table, all-ones = empty).
-__device__ __forceinline__ void dedup_min_insert(uint4* tab, uint32_t tmask, int x, int y, int z,
-                                                 uint32_t i, const DMap& M) {
-  const uint4 kEmpty = make_uint4(kNone, kNone, kNone, kNone);
-  const uint4 mine = make_uint4(uint32_t(x), uint32_t(y), uint32_t(z), i);
-  uint32_t h = cell_hash(x, y, z) & tmask;
-  for (uint32_t p = 0; p <= tmask; ++p, h = (h + 1) & tmask) {
-    const uint4 old = cas128(tab + h, kEmpty, mine);
-    if (eq4(old, kEmpty)) return;
-    if (key_eq(old, x, y, z)) {
-      atomicMin(&tab[h].w, i);
-      return;
-    }
-  }
-  set_err(M, ERR_SCRATCH);
-}
-
-__device__ __forceinline__ uint32_t dedup_lookup(const uint4* tab, uint32_t tmask, int x, int y,
-                                                 int z) {
-  uint32_t h = cell_hash(x, y, z) & tmask;
-  for (uint32_t p = 0; p <= tmask; ++p, h = (h + 1) & tmask) {
-    const uint4 b = tab[h];
-    if (b.w == kNone) return kNone;
-    if (key_eq(b, x, y, z)) return b.w;
-  }
-  return kNone;
-}
-
-// insertPointCloud's per-point math (probabilistic_map.hpp:144-156) in double
-// with one IEEE rounding per operation and no contraction:
-//   v = to - from; sq = (vx*vx + vy*vy) + vz*vz;
-//   sq >= max_range^2 ? miss at from + (v / sqrt(sq)) * max_range : hit at to
-// then posToCoord = floor(p * inv_resolution) (bonxai.hpp:404-410).
+// Endpoint of each point; lowest index per endpoint cell in the scratch table.
 template <typename PT>
 __global__ void k_endpoints(DMap M, const uint8_t* __restrict__ pts, size_t stride, uint32_t n,
                             double fx, double fy, double fz, double max_range, double mr2,
@@ -106,33 +35,9 @@ __global__ void k_endpoints(DMap M, const uint8_t* __restrict__ pts, size_t stri
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const PT* p = reinterpret_cast<const PT*>(pts + size_t(i) * stride);
-  const double tx = static_cast<double>(p[0]), ty = static_cast<double>(p[1]),
-               tz = static_cast<double>(p[2]);
-  if (!keep_nonfinite && !finite3(tx, ty, tz)) {
-    ep[i] = make_int4(0, 0, 0, EP_SKIP);
-    return;
-  }
-  const double vx = __dsub_rn(tx, fx), vy = __dsub_rn(ty, fy), vz = __dsub_rn(tz, fz);
-  const double sq = __dadd_rn(__dadd_rn(__dmul_rn(vx, vx), __dmul_rn(vy, vy)), __dmul_rn(vz, vz));
-  double ex, ey, ez;
-  int kind;
-  if (sq >= mr2) {
-    const double s = __dsqrt_rn(sq);
-    ex = __dadd_rn(fx, __dmul_rn(__ddiv_rn(vx, s), max_range));
-    ey = __dadd_rn(fy, __dmul_rn(__ddiv_rn(vy, s), max_range));
-    ez = __dadd_rn(fz, __dmul_rn(__ddiv_rn(vz, s), max_range));
-    kind = EP_MISS;
-  } else {
-    ex = tx;
-    ey = ty;
-    ez = tz;
-    kind = EP_HIT;
-  }
-  const int cx = __double2int_rd(__dmul_rn(ex, inv_res));
-  const int cy = __double2int_rd(__dmul_rn(ey, inv_res));
-  const int cz = __double2int_rd(__dmul_rn(ez, inv_res));
-  ep[i] = make_int4(cx, cy, cz, kind);
-  dedup_min_insert(tab, tmask, cx, cy, cz, i, M);
+  const int4 e = compute_endpoint<PT>(p, fx, fy, fz, max_range, mr2, inv_res, keep_nonfinite != 0);
+  ep[i] = e;
+  if (e.w != EP_SKIP) dedup_min_insert(tab, tmask, e.x, e.y, e.z, i, M);
 }
 
 // addHitPoint / addMissPoint batches: double points with a given kind, or a
@@ -150,33 +55,17 @@ __global__ void k_endpoints_kind(DMap M, const double* __restrict__ pts, uint32_
   dedup_min_insert(tab, tmask, cx, cy, cz, i, M);
 }
 
-__device__ __forceinline__ uint32_t chebyshev(int ox, int oy, int oz, int x, int y, int z) {
-  const uint32_t dx = static_cast<uint32_t>(abs(x - ox)), dy = static_cast<uint32_t>(abs(y - oy)),
-                 dz = static_cast<uint32_t>(abs(z - oz));
-  return max(dx, max(dy, dz));
-}
-
-// The lowest-index point of each endpoint cell decides: no update and no ray
-// if the cell exists with update_id == u, else it joins the ray list.
+// The lowest-index point of each endpoint cell decides and applies
+// (winner_apply) and, if its ray is cast, joins the ray list.
 __global__ void k_winners(DMap M, const int4* __restrict__ ep, uint32_t n,
                           const uint4* __restrict__ tab, uint32_t tmask, int ox, int oy, int oz,
-                          int32_t u, int4* __restrict__ cast, uint32_t cast_cap) {
+                          int32_t u, Opts o, int4* __restrict__ cast, uint32_t cast_cap) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   bool add = false;
   int4 e = make_int4(0, 0, 0, EP_SKIP);
   if (i < n) {
     e = ep[i];
-    if (e.w != EP_SKIP && dedup_lookup(tab, tmask, e.x, e.y, e.z) == i) {
-      add = true;
-      const uint32_t lf = leaf_of(M, e.x, e.y, e.z, false);
-      if (lf != kNone) {
-        const uint32_t ci = leaf_index(M, e.x, e.y, e.z);
-        if (cell_is_on(M, lf, ci)) {
-          const int32_t w = reinterpret_cast<const int32_t*>(M.ldata)[size_t(lf) * M.lsize + ci];
-          if (cell_id(w) == u) add = false;
-        }
-      }
-    }
+    if (e.w != EP_SKIP && dedup_lookup(tab, tmask, e.x, e.y, e.z) == i) add = winner_apply(M, e, u, o);
   }
   const unsigned lane = threadIdx.x & 31;
   const unsigned valid = __ballot_sync(0xffffffffu, i < n && e.w != EP_SKIP);
@@ -200,9 +89,9 @@ __global__ void k_winners(DMap M, const int4* __restrict__ ep, uint32_t n,
   }
 }
 
-// Creates each listed endpoint cell and applies its hit or miss
-// (probabilistic_map.cpp:35-41,49-54). Idempotent: a cell already at u is
-// left alone, so a retry after pool growth is safe.
+// Completes listed endpoints after a pool ran out: creates each cell and
+// applies its hit or miss (probabilistic_map.cpp:35-41,49-54). Idempotent --
+// a cell already at u is left alone -- so it may run over the whole list.
 __global__ void k_apply(DMap M, const int4* __restrict__ cast, uint32_t cast_cap, int32_t u,
                         Opts o) {
   const uint32_t n = min(ld_volatile(M.ctr + C_CAST), cast_cap);
@@ -223,18 +112,12 @@ __global__ void k_apply(DMap M, const int4* __restrict__ cast, uint32_t cast_cap
   }
 }
 
-// ---------------------------------------------------------------------------
-// ray phase
-// ---------------------------------------------------------------------------
-// One group of W lanes walks one ray; lane sl handles k = sl, sl+W, ...
-// Consecutive lanes hold consecutive cells, so the lanes of one step touch a
-// few leaves: the first lane of each leaf run (a "head") looks the leaf up or
-// creates it, and the others take its slot by shuffle. The group keeps the
-// last leaf and root between steps.
-template <int W>
-__global__ void __launch_bounds__(256) k_rays(DMap M, const int4* __restrict__ cast,
-                                              uint32_t cast_cap, int ox, int oy, int oz,
-                                              int32_t u, int32_t miss, int32_t cmin) {
+// Ray phase: one group of W lanes per listed ray (walk_ray, or walk_ray2 with
+// two cells per lane per step when U == 2).
+template <int W, int U>
+__global__ void __launch_bounds__(256, U == 2 ? 3 : 4) k_rays(DMap M, const int4* __restrict__ cast,
+                                                 uint32_t cast_cap, int ox, int oy, int oz,
+                                                 int32_t u, int32_t miss, int32_t cmin) {
   const uint32_t n_cast = min(ld_volatile(M.ctr + C_CAST), cast_cap);
   const unsigned lane = threadIdx.x & 31;
   const unsigned sl = lane & (W - 1);
@@ -242,87 +125,12 @@ __global__ void __launch_bounds__(256) k_rays(DMap M, const int4* __restrict__ c
   const unsigned gmask = (W == 32) ? 0xffffffffu : (((1u << W) - 1u) << gbase);
   const uint32_t gid = (blockIdx.x * blockDim.x + threadIdx.x) / W;
   const uint32_t ngroups = (gridDim.x * blockDim.x) / W;
-  const int32_t lm = leaf_mask(M);
-  const int32_t rm = root_mask(M);
   uint32_t visited = 0, updated = 0;
-
   for (uint32_t r = gid; r < n_cast; r += ngroups) {
-    const int4 e = cast[r];
-    const int dx = e.x - ox, dy = e.y - oy, dz = e.z - oz;
-    const uint32_t ax = static_cast<uint32_t>(abs(dx)), ay = static_cast<uint32_t>(abs(dy)),
-                   az = static_cast<uint32_t>(abs(dz));
-    const uint32_t m = max(ax, max(ay, az));
-    if (m == 0) continue;  // origin == end: no ray (probabilistic_map.hpp:164-166)
-    if (m >= kMaxRayCells) {
-      if (sl == 0) set_err(M, ERR_RAY_TOO_LONG);
-      continue;
-    }
-    const int sx = dx < 0 ? -1 : 1, sy = dy < 0 ? -1 : 1, sz = dz < 0 ? -1 : 1;
-    const uint32_t two_m = 2u * m;
-    const float rtm = __frcp_rn(static_cast<float>(two_m));
-    AxisStep X, Y, Z;
-    axis_init(X, ax, m, two_m, rtm, sl, W);
-    axis_init(Y, ay, m, two_m, rtm, sl, W);
-    axis_init(Z, az, m, two_m, rtm, sl, W);
-    int pkx = kEmptyKey, pky = kEmptyKey, pkz = kEmptyKey;  // group's last leaf key
-    uint32_t pleaf = kNone;
-    int rkx = kEmptyKey, rky = kEmptyKey, rkz = kEmptyKey;  // group's last root
-    uint32_t rin = kNone;
-
-    for (uint32_t base = 0; base < m; base += W) {
-      const bool act = base + sl < m;
-      const int cx = ox + sx * static_cast<int>(X.n);
-      const int cy = oy + sy * static_cast<int>(Y.n);
-      const int cz = oz + sz * static_cast<int>(Z.n);
-      const int lkx = cx & lm, lky = cy & lm, lkz = cz & lm;
-      int qx = __shfl_up_sync(gmask, lkx, 1, W);
-      int qy = __shfl_up_sync(gmask, lky, 1, W);
-      int qz = __shfl_up_sync(gmask, lkz, 1, W);
-      if (sl == 0) {
-        qx = pkx;
-        qy = pky;
-        qz = pkz;
-      }
-      const bool head = act && (lkx != qx || lky != qy || lkz != qz);
-      uint32_t leaf = kNone, in = kNone;
-      const int rx = cx & rm, ry = cy & rm, rz = cz & rm;
-      if (head) {
-        in = (rx == rkx && ry == rky && rz == rkz) ? rin : root_get_or_create(M, rx, ry, rz);
-        if (in != kNone) leaf = leaf_get_or_create(M, in, inner_index(M, cx, cy, cz), lkx, lky, lkz);
-      }
-      const unsigned hm = (__ballot_sync(gmask, head) & gmask) >> gbase;
-      const unsigned below = hm & ((2u << sl) - 1u);
-      const int src = below ? 31 - __clz(below) : 0;
-      const uint32_t got = __shfl_sync(gmask, leaf, src, W);
-      leaf = below ? got : pleaf;
-      if (hm) {  // remember the root of the highest head
-        const int hl = 31 - __clz(hm);
-        rkx = __shfl_sync(gmask, rx, hl, W);
-        rky = __shfl_sync(gmask, ry, hl, W);
-        rkz = __shfl_sync(gmask, rz, hl, W);
-        rin = __shfl_sync(gmask, in, hl, W);
-      }
-      if (act && leaf != kNone) {
-        const uint32_t ci = leaf_index(M, cx, cy, cz);
-        cell_mark_on(M, leaf, ci);
-        int32_t* cp = reinterpret_cast<int32_t*>(M.ldata) + size_t(leaf) * M.lsize + ci;
-        const int32_t w = *cp;
-        if (cell_id(w) != u) {
-          *cp = cell_pack(max(wrap_add(cell_prob(w), miss), cmin), u);
-          updated++;
-        }
-        visited++;
-      }
-      const uint32_t rem = m - base;
-      const int last = static_cast<int>(rem < W ? rem : W) - 1;
-      pkx = __shfl_sync(gmask, lkx, last, W);
-      pky = __shfl_sync(gmask, lky, last, W);
-      pkz = __shfl_sync(gmask, lkz, last, W);
-      pleaf = __shfl_sync(gmask, leaf, last, W);
-      axis_advance(X, two_m);
-      axis_advance(Y, two_m);
-      axis_advance(Z, two_m);
-    }
+    if (U == 2)
+      walk_ray2<W>(M, cast[r], ox, oy, oz, u, miss, cmin, sl, gbase, gmask, visited, updated);
+    else
+      walk_ray<W>(M, cast[r], ox, oy, oz, u, miss, cmin, sl, gbase, gmask, visited, updated);
   }
   visited = __reduce_add_sync(0xffffffffu, visited);
   updated = __reduce_add_sync(0xffffffffu, updated);
@@ -437,7 +245,7 @@ int endpoint_phase(bxg_pmap_s* pm, uint32_t n, int ox, int oy, int oz, Launch&& 
   BXG_LAUNCHED(m);
   record(pm, 1);
   k_winners<<<blocks, 256, 0, m->stream>>>(m->dm, m->s_ep.as<int4>(), n, m->s_dedup.as<uint4>(),
-                                           tcap - 1, ox, oy, oz, pm->update_count,
+                                           tcap - 1, ox, oy, oz, pm->update_count, opts_of(pm),
                                            m->s_cast.as<int4>(), uint32_t(m->s_cast.cap / 16));
   BXG_LAUNCHED(m);
   record(pm, 2);
@@ -469,19 +277,19 @@ int launch_rays(bxg_pmap_s* pm, int ox, int oy, int oz) {
   if (!blocks) return BXG_OK;
   const Opts o = opts_of(pm);
   const uint32_t ccap = uint32_t(m->s_cast.cap / 16);
-  switch (rpw) {
-    case 4:
-      k_rays<8><<<unsigned(blocks), bs, 0, m->stream>>>(m->dm, m->s_cast.as<int4>(), ccap, ox, oy, oz,
-                                                        pm->update_count, o.miss, o.cmin);
-      break;
-    case 2:
-      k_rays<16><<<unsigned(blocks), bs, 0, m->stream>>>(m->dm, m->s_cast.as<int4>(), ccap, ox, oy, oz,
-                                                         pm->update_count, o.miss, o.cmin);
-      break;
-    default:
-      k_rays<32><<<unsigned(blocks), bs, 0, m->stream>>>(m->dm, m->s_cast.as<int4>(), ccap, ox, oy, oz,
-                                                         pm->update_count, o.miss, o.cmin);
-      break;
+  const bool u2 = m->ray_unroll == 2;
+  const dim3 g{unsigned(blocks)}, b{unsigned(bs)};
+  const int4* c = m->s_cast.as<int4>();
+  const int32_t uc = pm->update_count;
+  if (rpw == 4) {
+    if (u2) k_rays<8, 2><<<g, b, 0, m->stream>>>(m->dm, c, ccap, ox, oy, oz, uc, o.miss, o.cmin);
+    else k_rays<8, 1><<<g, b, 0, m->stream>>>(m->dm, c, ccap, ox, oy, oz, uc, o.miss, o.cmin);
+  } else if (rpw == 2) {
+    if (u2) k_rays<16, 2><<<g, b, 0, m->stream>>>(m->dm, c, ccap, ox, oy, oz, uc, o.miss, o.cmin);
+    else k_rays<16, 1><<<g, b, 0, m->stream>>>(m->dm, c, ccap, ox, oy, oz, uc, o.miss, o.cmin);
+  } else {
+    if (u2) k_rays<32, 2><<<g, b, 0, m->stream>>>(m->dm, c, ccap, ox, oy, oz, uc, o.miss, o.cmin);
+    else k_rays<32, 1><<<g, b, 0, m->stream>>>(m->dm, c, ccap, ox, oy, oz, uc, o.miss, o.cmin);
   }
   BXG_LAUNCHED(m);
   return BXG_OK;
@@ -499,8 +307,10 @@ int finish_scan(bxg_pmap_s* pm, int ox, int oy, int oz, bool cast_rays, uint64_t
       unsigned long long* s = stats_of(m);
       BXG_CUDA(m, cudaMemsetAsync(s + S_VISITED, 0, 16, m->stream));
     }
-    st = launch_apply(pm);
-    if (st) return st;
+    if (attempt) {  // the winners applied the endpoints; complete them after growth
+      st = launch_apply(pm);
+      if (st) return st;
+    }
     record(pm, 3);
     if (cast_rays) {
       st = launch_rays(pm, ox, oy, oz);
@@ -562,8 +372,14 @@ int insert_impl(bxg_pmap m_, const PT* xyz, size_t stride, size_t n, const PT* o
                fz = static_cast<double>(origin[2]);
   int o[3];
   origin_coord(m, fx, fy, fz, o);
+  // Headroom for this scan's new leaves (twice the last scan's, at least a
+  // quarter of the points), so that the scan rarely has to grow and re-run.
+  const uint32_t leaves_before = m->h_ctr[C_LEAF];
+  int st = core_reserve(m, std::max<size_t>({size_t(2) * pm->last_new_leaves, n / 4, 1024}),
+                        std::max<size_t>(n / 64, 256));
+  if (st) return st;
   record(pm, 0);  // the scan's device time starts here
-  int st = reset_scan_stats(m);
+  st = reset_scan_stats(m);
   if (st) return st;
   if (n) {
     const void* dpts = nullptr;
@@ -581,8 +397,6 @@ int insert_impl(bxg_pmap m_, const PT* xyz, size_t stride, size_t n, const PT* o
   }
   if (!sync) {
     // asynchronous form: no retry; pools must have room (see core_maintain)
-    st = launch_apply(pm);
-    if (st) return st;
     st = launch_rays(pm, o[0], o[1], o[2]);
     if (st) return st;
     BXG_CUDA(m, cudaMemsetAsync(m->ctr.as<uint32_t>() + C_CAST, 0, 4, m->stream));
@@ -590,7 +404,10 @@ int insert_impl(bxg_pmap m_, const PT* xyz, size_t stride, size_t n, const PT* o
     if (++pm->update_count == 4) pm->update_count = 1;
     return BXG_OK;
   }
-  return finish_scan(pm, o[0], o[1], o[2], true, ray_cells, true);
+  st = finish_scan(pm, o[0], o[1], o[2], true, ray_cells, true);
+  if (!st)
+    pm->last_new_leaves = m->h_ctr[C_LEAF] > leaves_before ? m->h_ctr[C_LEAF] - leaves_before : 0;
+  return st;
 }
 
 int add_points(bxg_pmap m_, const double* xyz, size_t n, int kind,
@@ -650,6 +467,35 @@ int query(bxg_pmap m_, const int32_t* xyz, size_t n, uint8_t* out, int mode) {
 }  // namespace
 
 namespace bxg {
+int pmap_complete_scan(bxg_pmap_s* pm, const int4* d_cast, const uint32_t* d_count, uint32_t cap,
+                       int ox, int oy, int oz, int32_t u) {
+  MapCore* m = &pm->core;
+  cudaSetDevice(m->device);
+  const Opts o = opts_of(pm);
+  uint32_t err = 0;
+  int st = core_sync(m, &err);  // reads and clears what the tick left
+  if (st && !(err & (ERR_POOL_INNER | ERR_POOL_LEAF | ERR_HASH_FULL))) return st;
+  BXG_CUDA(m, cudaMemcpyAsync(m->ctr.as<uint32_t>() + C_CAST, d_count, 4,
+                              cudaMemcpyDeviceToDevice, m->stream));
+  for (int attempt = 0; attempt < 12 && err; attempt++) {
+    st = core_grow_for(m, err);
+    if (st) return st;
+    const unsigned ablocks = unsigned(std::min<uint64_t>((cap + 255) / 256, uint64_t(m->sm_count) * 8));
+    k_apply<<<std::max(ablocks, 1u), 256, 0, m->stream>>>(m->dm, d_cast, cap, u, o);
+    BXG_LAUNCHED(m);
+    const unsigned rblocks = unsigned(std::min<uint64_t>((cap + 7) / 8, uint64_t(m->sm_count) * 8));
+    k_rays<32, 1><<<std::max(rblocks, 1u), 256, 0, m->stream>>>(m->dm, d_cast, cap, ox, oy, oz,
+                                                               u, o.miss, o.cmin);
+    BXG_LAUNCHED(m);
+    st = core_sync(m, &err);
+    if (st && !(err & (ERR_POOL_INNER | ERR_POOL_LEAF | ERR_HASH_FULL))) return st;
+  }
+  BXG_CUDA(m, cudaMemsetAsync(m->ctr.as<uint32_t>() + C_CAST, 0, 4, m->stream));
+  BXG_CUDA(m, cudaStreamSynchronize(m->stream));
+  if (err) return set_error(m, BXG_ERR_OUT_OF_POOL, "pools could not grow enough");
+  return BXG_OK;
+}
+
 const MapCore* core_of_handle(const void* handle) {
   // Both handle types hold their MapCore as first member.
   return reinterpret_cast<const MapCore*>(handle);

@@ -62,6 +62,7 @@ typedef struct {
   uint32_t rays_per_warp;   /* ray kernel: rays per warp 1, 2 or 4; 0 = autotuned */
   uint32_t block_size;      /* ray kernel threads per block; 0 = autotuned */
   uint32_t flags;           /* BXG_FLAG_* */
+  uint32_t ray_unroll;      /* ray kernel: cells per lane per step, 1 or 2; 0 = autotuned */
 } bxg_config;
 
 /* Drop points with a NaN or infinite coordinate before insertion, as the
@@ -70,6 +71,8 @@ typedef struct {
 #define BXG_FLAG_KEEP_NONFINITE 1u
 /* Record CUDA events around each kernel (see bxg_pmap_kernel_times). */
 #define BXG_FLAG_TIMING 2u
+/* Batched ticks: launch directly instead of replaying a captured CUDA graph. */
+#define BXG_FLAG_NO_GRAPH 4u
 
 void bxg_config_default(bxg_config* cfg);
 const char* bxg_status_string(int status);
@@ -246,6 +249,101 @@ void* bxg_pmap_stream(bxg_pmap m);
  * (value_bytes 4, the packed CellT word) over the map's own pools. Valid while
  * the map lives; never pass it to bxg_grid_destroy. */
 bxg_grid bxg_pmap_grid(bxg_pmap m);
+
+/* ========================================================================
+ * Batched scans: insertPointCloud (probabilistic_map.hpp:141-160) on many
+ * independent maps at once -- one scan per map per call, all maps' phases in
+ * one persistent launch replayed from a CUDA graph. Each map ends bit-identical
+ * to inserting its scan alone; the maps must live on the batch's device and
+ * have no rays queued by bxg_pmap_add_*_points.
+ * ======================================================================== */
+typedef struct bxg_batch_s* bxg_batch;
+
+/* cfg: device, rays_per_warp (1, 2 or 4) and flags (BXG_FLAG_NO_GRAPH). */
+int bxg_batch_create(bxg_batch* out, const bxg_config* cfg);
+int bxg_batch_destroy(bxg_batch b);
+const char* bxg_batch_last_error(bxg_batch b);
+/* One tick: scan s (s < n_scans <= 128) inserts points
+ * xyz[3*offsets[s] .. 3*offsets[s+1]) (packed float, host or device memory)
+ * into maps[s] from origins[3*s..3*s+2] with max_ranges[s]. ray_cells
+ * (optional, n_scans) receives each scan's ray-cell updates. A map whose pool
+ * runs out during the tick is completed by the per-map path after it grows. */
+int bxg_batch_insert_f32(bxg_batch b, const bxg_pmap* maps, size_t n_scans, const float* xyz,
+                         const uint64_t* offsets, const float* origins, const double* max_ranges,
+                         uint64_t* ray_cells);
+/* Last tick: [0] device ms, [1] ran as a CUDA graph, [2] maps completed after
+ * a pool ran out, [3] ticks so far, [4] persistent grid (blocks), [5] tick
+ * launches so far, [6] endpoint phase ms, [7] winner + ray phases ms. */
+int bxg_batch_stats(bxg_batch b, double out[8]);
+/* Last tick's phases in ms (device global timer): [0] clear, [1] endpoints,
+ * [2] winners, [3] ray-list prefix, [4] rays. */
+int bxg_batch_phase_ms(bxg_batch b, double out[5]);
+
+/* ========================================================================
+ * Serving: many clients, each with a persistent map on the device, sending
+ * insertPointCloud / isOccupied / getOccupiedVoxels requests
+ * (probabilistic_map.hpp:91-124). A worker thread batches whatever is queued
+ * into ticks (continuous batching); requests on one map run in submission
+ * order and see exactly the state they would see alone. Admission: insert
+ * slots and points per tick, and an HBM budget across all maps' node pools.
+ * ======================================================================== */
+typedef struct bxg_server_s* bxg_server;
+
+typedef struct {
+  size_t pool_budget_bytes;      /* across all maps' node pools; 0 = 40 GiB */
+  uint32_t max_scans_per_tick;   /* insert slots per tick (<= 128); 0 = 128 */
+  uint64_t max_points_per_tick;  /* 0 = 64 Mi points */
+  uint64_t max_lookups_per_tick; /* 0 = 64 Mi coordinates */
+  int device;                    /* -1 = current */
+  uint32_t rays_per_warp;        /* batched ray kernel, 1/2/4 */
+  uint32_t ray_unroll;           /* batched ray kernel, 1/2 */
+  uint32_t flags;                /* BXG_FLAG_* for the maps and the batch */
+  uint32_t initial_leaves;       /* per map; 0 = 4096 */
+} bxg_server_config;
+
+typedef struct {
+  int status;        /* bxg_status of the request */
+  int kind;          /* 0 insert, 1 lookup, 2 getOccupiedVoxels */
+  uint32_t map;
+  uint64_t ray_cells;/* inserts: ray-cell updates */
+  size_t n_out;      /* lookups: answers; getOccupiedVoxels: coordinates */
+  double latency_ms; /* submission to completion */
+  double queue_ms;   /* submission to the start of its tick */
+  uint64_t tick;
+} bxg_server_result;
+
+void bxg_server_config_default(bxg_server_config* cfg);
+/* One map per client, resolutions[i] for map i; starts the worker thread. */
+int bxg_server_create(bxg_server* out, const double* resolutions, size_t n_maps,
+                      const bxg_server_config* cfg);
+/* Stops the worker after the queued requests (waits for them). */
+int bxg_server_destroy(bxg_server s);
+const char* bxg_server_last_error(bxg_server s);
+/* Submissions copy their inputs and return a ticket. With discard != 0 the
+ * result is dropped on completion (only its latency is recorded) and the
+ * ticket cannot be waited for. */
+int bxg_server_insert(bxg_server s, uint32_t map, const float* xyz, size_t n,
+                      const float origin[3], double max_range, int discard, uint64_t* ticket);
+/* mode 0 isOccupied, 1 isUnknown, 2 isFree. */
+int bxg_server_query(bxg_server s, uint32_t map, const int32_t* xyz, size_t n, int mode,
+                     int discard, uint64_t* ticket);
+int bxg_server_get_occupied(bxg_server s, uint32_t map, int discard, uint64_t* ticket);
+/* Waits for a ticket; copies lookup answers (cap bytes) or occupied
+ * coordinates (cap coordinates) to out and releases the ticket. With
+ * out == NULL a lookup or getOccupiedVoxels ticket is kept: res->n_out tells
+ * the size to allocate for a second call. */
+int bxg_server_wait(bxg_server s, uint64_t ticket, double timeout_s, bxg_server_result* res,
+                    void* out, size_t cap);
+/* Waits until every submitted request has completed. */
+int bxg_server_drain(bxg_server s, double timeout_s);
+/* [0] completed [1] inserts [2] lookups [3] occupied [4] ticks [5] p50 ms
+ * [6] p99 ms [7] insert p50 [8] insert p99 [9] lookup p50 [10] lookup p99
+ * [11] ray-cell updates [12] lookup coordinates [13] rejected [14] busy s
+ * [15] first submission to last completion s [16] occupied p50 [17] occupied
+ * p99 [18] pool bytes of all maps [19] reserved. */
+int bxg_server_stats(bxg_server s, double out[20]);
+/* The map of one client (for inspection after bxg_server_drain). */
+bxg_pmap bxg_server_map(bxg_server s, uint32_t map);
 
 /* ComputeRay(origin, end) (probabilistic_map.hpp:13-19,162-203) on the GPU for
  * n rays: out_len[i] = ray length; cells of ray i are written at

@@ -6,7 +6,7 @@
 // the CPU oracle.
 //
 // usage: dropin_main <scans.bin> <out_dir>
-//   scans.bin: int32 n_scans, int32 n_points, float resolution, float max_range,
+//   scans.bin: int32 n_scans, int32 n_points, double resolution, double max_range,
 //              then per scan: float origin[3], float xyz[n_points*3]
 #include <cstdio>
 #include <fstream>
@@ -84,11 +84,11 @@ static int tutorial(const std::string& out) {
 static int lidar(const std::string& in, const std::string& outdir) {
   std::ifstream f(in, std::ios::binary);
   int32_t n_scans = 0, n_points = 0;
-  float res = 0, max_range = 0;
+  double res = 0, max_range = 0;
   f.read(reinterpret_cast<char*>(&n_scans), 4);
   f.read(reinterpret_cast<char*>(&n_points), 4);
-  f.read(reinterpret_cast<char*>(&res), 4);
-  f.read(reinterpret_cast<char*>(&max_range), 4);
+  f.read(reinterpret_cast<char*>(&res), 8);
+  f.read(reinterpret_cast<char*>(&max_range), 8);
   Bonxai::ProbabilisticMap map(res);
   std::vector<float> buf(size_t(n_points) * 3);
   for (int s = 0; s < n_scans; s++) {

@@ -18,7 +18,11 @@ ROOT = Path(__file__).resolve().parent.parent
 def dropin_exe(tmp_path_factory, cuda_lib):
     out = tmp_path_factory.mktemp("dropin") / "dropin_main"
     lib_dir = ROOT / "bonxai_gb300" / "_build"
-    subprocess.check_call(["g++", "-std=c++17", "-O2", "-Wall", "-Wextra", "-Werror",
+    # -ffp-contract=off: the program computes its own test points (e.g.
+    # -0.5 + 0.3 * a); GCC on aarch64 would fuse those into FMAs by default and
+    # the points would differ by an ulp from the oracle replay below.
+    subprocess.check_call(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-Wall", "-Wextra",
+                           "-Werror",
                            f"-I{ROOT / 'include'}", str(ROOT / "tests" / "cpp" / "dropin_main.cpp"),
                            f"-L{lib_dir}", "-lbonxai_gb300", f"-Wl,-rpath,{lib_dir}", "-o", str(out)])
     return out
@@ -30,7 +34,7 @@ def test_dropin_program_matches_oracle(dropin_exe, tmp_path, port):
     scans = [scene.scan(k, n_points=n_pts) for k in range(n_scans)]
     with open(tmp_path / "scans.bin", "wb") as f:
         np.array([n_scans, n_pts], np.int32).tofile(f)
-        np.array([scene.resolution, scene.max_range], np.float32).tofile(f)
+        np.array([scene.resolution, scene.max_range], np.float64).tofile(f)
         for pts, o in scans:
             o.astype(np.float32).tofile(f)
             pts.astype(np.float32).tofile(f)

@@ -59,10 +59,10 @@ def test_golden_add_points(gpu):
     assert np.array_equal(xyz, g["xyz"]) and np.array_equal(c, g["cells"])
 
 
-@pytest.mark.parametrize("rpw", [1, 2, 4])
-def test_lidar_scans_vs_oracle(gpu, port, rpw):
+@pytest.mark.parametrize("rpw,unroll", [(1, 1), (2, 1), (4, 1), (1, 2), (2, 2), (4, 2)])
+def test_lidar_scans_vs_oracle(gpu, port, rpw, unroll):
     scene = synth.LidarScene()
-    m = gpu.ProbabilisticMap(scene.resolution, gpu.Config(rays_per_warp=rpw))
+    m = gpu.ProbabilisticMap(scene.resolution, gpu.Config(rays_per_warp=rpw, ray_unroll=unroll))
     o = port.pmap(scene.resolution)
     for k in range(5):
         pts, org = scene.scan(k, n_points=16384)
