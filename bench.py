@@ -221,8 +221,8 @@ def run_ours(args):
     h_scans = [(torch.from_numpy(p).pin_memory(), o) for p, o in scans]
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device=dev)
 
-    cfg = bx.Config(flags=bx.FLAG_TIMING, rays_per_warp=args.rays_per_warp,
-                    ray_unroll=args.ray_unroll,
+    cfg = bx.Config(flags=bx.FLAG_TIMING | args.ray_flags, rays_per_warp=args.rays_per_warp,
+                    ray_unroll=args.ray_unroll, block_size=args.block_size,
                     initial_leaves=1 << 19, initial_inners=1 << 15, hash_buckets=1 << 15)
     m = bx.ProbabilisticMap(scene.resolution, cfg)
     mr = scene.max_range
@@ -353,6 +353,245 @@ def run_ours(args):
     if ws > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+    return 0
+
+
+# ----------------------------------------------------------------------------
+# room workload: VoxelGrid<float> create / update / iterate (300k points)
+# ----------------------------------------------------------------------------
+def run_room(args):
+    """VoxelGrid<float> at 0.02 m, (2,3) bits, 300,000 points of a 6x4x3 m room
+    with 20 spheres: create (setValue of U[0,1) values at posToCoord of the
+    points on a cleared grid), update (setValue of new values), iterate
+    (forEachCell as a dump of coordinates and values into device buffers).
+    One step = the three phases; metric = grid items/s = (2 x points + cells
+    dumped) / device time."""
+    import ctypes as C
+    import torch
+    import bonxai_gb300 as bx
+    from bonxai_gb300 import synth
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local if ws > 1 else 0)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    s = torch.cuda.Stream()
+    pts = synth.room_cloud(300_000, seed=1000)
+    g0 = bx.VoxelGrid(0.02, 2, 3, np.float32)
+    coords = torch.from_numpy(g0.pos_to_coord(pts)).to(dev)
+    g0.close()
+    vals = [torch.from_numpy(synth.room_values(len(pts), seed=1000 + k)).to(dev)
+            for k in range(2)]
+    g = bx.VoxelGrid(0.02, 2, 3, np.float32,
+                     bx.Config(stream=s.cuda_stream, initial_leaves=1 << 14))
+    lib = g.lib
+    n = len(pts)
+    out_xyz = torch.empty((n, 3), dtype=torch.int32, device=dev)
+    out_val = torch.empty(n, dtype=torch.float32, device=dev)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device=dev)
+    got = C.c_size_t()
+
+    def step(k):
+        g.clear()
+        flush.fill_(k)
+        torch.cuda.synchronize()
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        e[0].record(s)
+        g._check(lib.bxg_grid_set_values(g.h, C.c_void_p(coords.data_ptr()),
+                                         C.c_void_p(vals[0].data_ptr()), n, None))
+        e[1].record(s)
+        g._check(lib.bxg_grid_set_values(g.h, C.c_void_p(coords.data_ptr()),
+                                         C.c_void_p(vals[1].data_ptr()), n, None))
+        e[2].record(s)
+        g._check(lib.bxg_grid_dump(g.h, C.c_void_p(out_xyz.data_ptr()),
+                                   C.c_void_p(out_val.data_ptr()), n, C.byref(got)))
+        e[3].record(s)
+        torch.cuda.synchronize()
+        return [e[i].elapsed_time(e[i + 1]) for i in range(3)], got.value
+
+    for k in range(args.warmup):
+        step(k)
+    phase = np.zeros(3)
+    cells = 0
+    with ClockSampler(dev.index) as clk:
+        for k in range(args.steps):
+            t, c = step(k)
+            phase += t
+            cells = c
+    clocks = clk.summary()
+    ms = float(phase.sum()) / args.steps
+    items = 2 * n + cells
+    value = items / (ms / 1e3)
+    roots, leaves = g.node_counts()
+    # algorithmic bytes: create 16 B/point in + 4 B/cell written + 64 B mask per
+    # leaf; update 16 B/point + 4 B/cell; iterate 64 B mask per leaf + 4 B per
+    # cell read + 16 B per cell out
+    b_create = 16 * n + 4 * cells + 64 * leaves
+    b_update = 16 * n + 4 * cells
+    b_iter = 64 * leaves + 20 * cells
+    pk, pkind = peaks()
+    ph = phase / args.steps
+    dom = int(np.argmax(ph))
+    b_dom = [b_create, b_update, b_iter][dom]
+    ach = b_dom / (ph[dom] / 1e3) / 1e9
+    # e2e: host coordinates and values through the C ABI, dump to host
+    h_coords = coords.cpu().numpy()
+    h_vals = [v.cpu().numpy() for v in vals]
+    h_xyz = np.empty((n, 3), np.int32)
+    h_out = np.empty(n, np.float32)
+    t_e2e = 0.0
+    for k in range(args.steps):
+        g.clear()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        g._check(lib.bxg_grid_set_values(g.h, h_coords.ctypes.data_as(C.c_void_p),
+                                         h_vals[0].ctypes.data_as(C.c_void_p), n, None))
+        g._check(lib.bxg_grid_set_values(g.h, h_coords.ctypes.data_as(C.c_void_p),
+                                         h_vals[1].ctypes.data_as(C.c_void_p), n, None))
+        g._check(lib.bxg_grid_dump(g.h, h_xyz.ctypes.data_as(C.c_void_p),
+                                   h_out.ctypes.data_as(C.c_void_p), n, C.byref(got)))
+        t_e2e += time.perf_counter() - t0
+    e2e = items * args.steps / t_e2e
+    cpu = None
+    if not args.no_cpu:
+        from oracle import oracle as O
+        port = O.port()
+        og = port.grid(0.02, 2, 3, O.ORC_F32)
+        t0 = time.perf_counter()
+        og.set_values(h_coords, h_vals[0])
+        og.set_values(h_coords, h_vals[1])
+        xyz_c, _ = og.dump()
+        tc = time.perf_counter() - t0
+        cpu = {"value": (2 * n + len(xyz_c)) / tc, "unit": "grid items/s", "cores": 1,
+               "kind": "port", "sample": f"one create+update+iterate, one thread, {tc:.2f} s"}
+    if rank != 0:
+        return 0
+    line = {
+        "metric": "grid items/s (setValue create + update + forEachCell)", "value": value,
+        "unit": "grid items/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "room_300k_voxelgrid_float", "points": n, "resolution_m": 0.02,
+                   "inner_bits": 2, "leaf_bits": 3, "room": "6x4x3 m, 20 spheres",
+                   "l2": "flushed before every step (256 MiB write); the grid (~"
+                         f"{(leaves * 2112) >> 20} MiB) fits L2, so phases 2-3 hit it",
+                   "parallelism": f"replicas x{ws}"},
+        "phase_ms": {"create": ph[0], "update": ph[1], "iterate": ph[2]},
+        "cells": cells, "leaves": leaves, "roots": roots,
+        "roofline": {"kernel": ["create", "update", "iterate"][dom], "bound": "hbm",
+                     "achieved": ach, "peak": pk, "unit": "GB/s", "frac": ach / pk,
+                     "peak_kind": pkind, "traffic": None,
+                     "algorithmic_bytes_per_launch": b_dom},
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e, "unit": "grid items/s",
+                "h2d_bytes_per_step": 2 * n * 16, "d2h_bytes_per_step": cells * 16},
+        "gpu_launches": None, "clocks": clocks,
+    }
+    print(json.dumps(line), flush=True)
+    g.close()
+    return 0
+
+
+# ----------------------------------------------------------------------------
+# depth workload: 640x480 camera frames, then 1 M isOccupied lookups
+# ----------------------------------------------------------------------------
+def run_depth(args):
+    """ProbabilisticMap at 0.02 m, max_range 5 m: 640x480 pinhole depth frames
+    (fx = fy = 525) of an 8x6x3 m room with 50 boxes along a 6-DoF random walk
+    (one step = one frame, invalid pixels dropped), then isOccupied on 1 M
+    coordinates drawn uniformly in the final map's cell box. value = ray-cell
+    updates/s of the frames; "lookup" = the lookups, device-resident."""
+    import ctypes as C
+    import torch
+    import bonxai_gb300 as bx
+    from bonxai_gb300 import synth
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local if ws > 1 else 0)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    room = synth.DepthRoom()
+    n_frames = max(args.steps, 1) + args.warmup
+    frames = [room.frame(k) for k in range(n_frames)]
+    d_frames = [(torch.from_numpy(p).to(dev), o) for p, o in frames]
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device=dev)
+    m = bx.ProbabilisticMap(room.resolution,
+                            bx.Config(flags=bx.FLAG_TIMING | args.ray_flags,
+                                      rays_per_warp=args.rays_per_warp,
+                                      ray_unroll=args.ray_unroll, initial_leaves=1 << 18))
+    for k in range(args.warmup):
+        m.insert_point_cloud(*d_frames[k], room.max_range)
+    m.clear()
+    V, ms, ray_ms = 0, 0.0, []
+    with ClockSampler(dev.index) as clk:
+        for k in range(args.steps):
+            flush.fill_(k)
+            torch.cuda.synchronize()
+            V += m.insert_point_cloud(*d_frames[args.warmup + k], room.max_range)
+            t = m.kernel_times()
+            ms += sum(t)
+            ray_ms.append(t[3])
+    clocks = clk.summary()
+    value = V / (ms / 1e3)
+    xyz, _ = m.dump(sort=False)
+    q = torch.from_numpy(synth.lookup_coords(xyz.min(0), xyz.max(0), 1 << 20, seed=3)).to(dev)
+    out = torch.empty(q.shape[0], dtype=torch.uint8, device=dev)
+    s = torch.cuda.ExternalStream(m.stream)
+    lib = m.lib
+    look = []
+    for k in range(args.warmup + args.steps):
+        flush.fill_(k)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(s)
+        m._check(lib.bxg_pmap_is_occupied(m.h, C.c_void_p(q.data_ptr()), q.shape[0],
+                                          C.c_void_p(out.data_ptr())))
+        b.record(s)
+        torch.cuda.synchronize()
+        if k >= args.warmup:
+            look.append(a.elapsed_time(b))
+    lk_ms = float(np.median(look))
+    nq = q.shape[0]
+    pk, pkind = peaks()
+    lk_ach = 17.0 * nq / (lk_ms / 1e3) / 1e9
+    # e2e: host points through the C ABI
+    t_e2e, V_e2e = 0.0, 0
+    m.clear()
+    for k in range(args.steps):
+        p, o = frames[args.warmup + k]
+        t0 = time.perf_counter()
+        V_e2e += m.insert_point_cloud(p, o, room.max_range)
+        t_e2e += time.perf_counter() - t0
+    cpu = None
+    if not args.no_cpu:
+        from oracle import oracle as O
+        om = O.port().pmap(room.resolution)
+        t0 = time.perf_counter()
+        Vc = sum(om.insert(*frames[args.warmup + k], room.max_range) for k in range(min(3, args.steps)))
+        tc = time.perf_counter() - t0
+        cpu = {"value": Vc / tc, "unit": "ray-cell updates/s", "cores": 1, "kind": "port",
+               "sample": f"{min(3, args.steps)} frames, one thread, {tc:.2f} s"}
+    if rank != 0:
+        return 0
+    line = {
+        "metric": "ray-cell updates/s", "value": value, "unit": "ray-cell updates/s",
+        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+        "config": {"workload": "depth_640x480_room", "resolution_m": room.resolution,
+                   "max_range_m": room.max_range, "camera": "640x480, fx=fy=525",
+                   "room": "8x6x3 m, 50 boxes", "frames": args.steps,
+                   "l2": "flushed before every timed frame and lookup batch",
+                   "parallelism": f"replicas x{ws}"},
+        "lookup": {"lookups_per_s": nq / (lk_ms / 1e3), "n": nq, "ms": lk_ms,
+                   "roofline": {"bound": "hbm", "achieved": lk_ach, "peak": pk, "unit": "GB/s",
+                                "frac": lk_ach / pk, "peak_kind": pkind,
+                                "algorithmic_bytes_per_lookup": 17,
+                                "random_access_achieved_gbs": 109.0 * nq / (lk_ms / 1e3) / 1e9}},
+        "roofline": None, "ray_kernel_ms": float(np.mean(ray_ms)),
+        "cpu_baseline": cpu,
+        "e2e": {"value": V_e2e / t_e2e, "unit": "ray-cell updates/s",
+                "h2d_bytes_per_step": int(np.mean([len(f[0]) for f in frames])) * 12,
+                "d2h_bytes_per_step": 128},
+        "gpu_launches": None, "clocks": clocks,
+    }
+    print(json.dumps(line), flush=True)
     return 0
 
 
@@ -579,14 +818,18 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="lidar", choices=["lidar", "multimap", "serve"])
+    ap.add_argument("--workload", default="lidar",
+                    choices=["lidar", "multimap", "serve", "room", "depth"])
     ap.add_argument("--maps", type=int, default=64)
     ap.add_argument("--clients", type=int, default=32)
     ap.add_argument("--rate", type=float, default=2000.0, help="offered requests/s (serve)")
     ap.add_argument("--duration", type=float, default=20.0, help="seconds of load (serve)")
     ap.add_argument("--budget-gb", type=int, default=40)
     ap.add_argument("--rays-per-warp", type=int, default=1)
-    ap.add_argument("--ray-unroll", type=int, default=1)
+    ap.add_argument("--ray-unroll", type=int, default=2)
+    ap.add_argument("--block-size", type=int, default=0)
+    ap.add_argument("--ray-flags", type=int, default=0,
+                    help="BXG_FLAG_RAY_CHUNKS (8) | BXG_FLAG_LEAF_CACHE (16)")
     ap.add_argument("--cpu-scans", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true",
@@ -597,6 +840,10 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "room":
+        return run_room(args)
+    if args.workload == "depth":
+        return run_depth(args)
     if args.workload == "multimap":
         return run_multimap(args)
     if args.workload == "serve":

@@ -32,6 +32,8 @@ SET_ALL_CELLS_OFF = 1
 FLAG_KEEP_NONFINITE = 1
 FLAG_TIMING = 2
 FLAG_NO_GRAPH = 4
+FLAG_RAY_CHUNKS = 8
+FLAG_LEAF_CACHE = 16
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "node pool exhausted", 3: "root hash full",
           4: "device wait timed out", 5: "CUDA error", 6: "no CUDA device",
@@ -89,6 +91,8 @@ _SIGS = {
     "bxg_grid_clear": (_int, [_vp, _int]),
     "bxg_grid_release_unused": (_int, [_vp]),
     "bxg_grid_synchronize": (_int, [_vp]),
+    "bxg_grid_serialize": (_int, [_vp, C.c_char_p, _vp, _sz, _vp]),
+    "bxg_grid_deserialize": (_int, [_vp, _vp, _sz]),
     "bxg_pmap_create": (_int, [_vp, _dbl, _vp]),
     "bxg_pmap_destroy": (_int, [_vp]),
     "bxg_pmap_get_options": (_int, [_vp, _vp]),
@@ -103,6 +107,8 @@ _SIGS = {
     "bxg_pmap_is_unknown": (_int, [_vp, _vp, _sz, _vp]),
     "bxg_pmap_is_free": (_int, [_vp, _vp, _sz, _vp]),
     "bxg_pmap_get_occupied": (_int, [_vp, _vp, _sz, _vp]),
+    "bxg_pmap_export_occupied_f32": (_int, [_vp, _vp, _sz, _vp, _dbl, _dbl]),
+    "bxg_pmap_insert_sensor_cloud_f32": (_int, [_vp, _vp, _sz, _sz, _vp, _dbl, _vp]),
     "bxg_pmap_get_free": (_int, [_vp, _vp, _sz, _vp]),
     "bxg_pmap_dump": (_int, [_vp, _vp, _vp, _sz, _vp]),
     "bxg_pmap_active_cells": (_int, [_vp, _vp]),
@@ -350,6 +356,28 @@ class VoxelGrid(_Handle):
     def release_unused_memory(self):
         self._check(self.lib.bxg_grid_release_unused(self.h))
 
+    _TYPE_NAMES = {np.dtype(np.float32): "float", np.dtype(np.float64): "double",
+                   np.dtype(np.int32): "int", np.dtype(np.uint32): "unsigned int",
+                   np.dtype(np.int64): "long", np.dtype(np.uint64): "unsigned long",
+                   np.dtype(np.int16): "short", np.dtype(np.uint16): "unsigned short",
+                   np.dtype(np.int8): "signed char", np.dtype(np.uint8): "unsigned char"}
+
+    def serialize(self, type_name: str | None = None) -> bytes:
+        """Serialize in the reference's byte format (serialization.hpp:77-116)."""
+        if type_name is None:
+            type_name = "Bonxai::EmptyVoxel" if self.dtype is None else self._TYPE_NAMES[self.dtype]
+        n = C.c_size_t()
+        st = self.lib.bxg_grid_serialize(self.h, type_name.encode(), None, 0, C.byref(n))
+        if st not in (0, 7):
+            self._check(st)
+        buf = C.create_string_buffer(n.value)
+        self._check(self.lib.bxg_grid_serialize(self.h, type_name.encode(), buf, n.value,
+                                                C.byref(n)))
+        return buf.raw[:n.value]
+
+    def deserialize(self, data: bytes):
+        self._check(self.lib.bxg_grid_deserialize(self.h, data, len(data)))
+
     releaseUnusedMemory = release_unused_memory
 
 
@@ -406,6 +434,18 @@ class ProbabilisticMap(_Handle):
         return v.value
 
     insertPointCloud = insert_point_cloud
+
+    def insert_sensor_cloud(self, points, sensor_to_world, max_range: float) -> int:
+        """The ROS node's ingest fused into one scan (bonxai_server.cpp:140-182):
+        sensor-frame float points, a 3x4 or 4x4 sensor-to-world transform;
+        non-finite points are dropped, the origin is the translation, and a
+        negative max_range means no limit. Returns V."""
+        p, keep, n = _in(points, np.float32, 3)
+        m = np.ascontiguousarray(np.asarray(sensor_to_world, np.float32)[:3, :4].reshape(12))
+        v = C.c_uint64()
+        self._check(self.lib.bxg_pmap_insert_sensor_cloud_f32(self.h, p, 0, n, _ptr(m),
+                                                              float(max_range), C.byref(v)))
+        return v.value
 
     def insert_point_cloud_async(self, points, origin, max_range: float):
         p, keep, n = _in(points, np.float32, 3)
@@ -492,6 +532,30 @@ class ProbabilisticMap(_Handle):
         return self._coords(self.lib.bxg_pmap_get_free, sort)
 
     getOccupiedVoxels, getFreeVoxels = get_occupied_voxels, get_free_voxels
+
+    def export_occupied(self, min_z=-np.inf, max_z=np.inf, out=None, sort: bool = True):
+        """Occupied corner positions (float xyz) with min_z <= z <= max_z, as
+        the ROS node publishes them. With out = a CUDA float32 tensor [cap, 3]
+        the positions stay on the GPU and the count is returned instead."""
+        got = C.c_size_t()
+        if out is not None:
+            st = self.lib.bxg_pmap_export_occupied_f32(self.h, _ptr(out), out.shape[0],
+                                                       C.byref(got), float(min_z), float(max_z))
+            if st not in (0, 7):
+                self._check(st)
+            return got.value
+        st = self.lib.bxg_pmap_export_occupied_f32(self.h, None, 0, C.byref(got),
+                                                   float(min_z), float(max_z))
+        if st not in (0, 7):
+            self._check(st)
+        n = got.value
+        pts = np.zeros((max(n, 1), 3), np.float32)
+        self._check(self.lib.bxg_pmap_export_occupied_f32(self.h, _ptr(pts), n, C.byref(got),
+                                                          float(min_z), float(max_z)))
+        pts = pts[:got.value]
+        if sort:
+            pts = pts[np.lexsort((pts[:, 2], pts[:, 1], pts[:, 0]))]
+        return pts
 
     def dump(self, sort: bool = True):
         """Every cell as (coords [n,3] int32, packed CellT words [n] int32)."""

@@ -1,6 +1,10 @@
-// Map lifecycle, node pools and their growth, counters, staging, iteration.
+// Map lifecycle, node pools and their growth, counters, staging, iteration,
+// serialization.
 #include <algorithm>
+#include <array>
 #include <cstdio>
+#include <cstdlib>
+#include <string>
 
 #include "bxg_internal.h"
 
@@ -414,23 +418,36 @@ int core_maintain(MapCore* m) {
   return BXG_OK;
 }
 
+// Headroom before a scan, best effort: a request the HBM budget does not
+// allow is skipped (the scan then grows on demand or reports the budget
+// itself); only CUDA errors are returned.
 int core_reserve(MapCore* m, size_t leaves, size_t inners) {
+  const std::string saved = m->err;
+  auto soft = [&](int st) -> int {
+    if (st == BXG_ERR_OUT_OF_POOL || st == BXG_ERR_HASH_FULL) {
+      m->err = saved;
+      return BXG_OK;
+    }
+    return st;
+  };
   const size_t lused = m->h_ctr[C_LEAF], lfree = m->h_ctr[C_FREE_LEAF];
   const size_t lavail = (m->dm.lcap > lused ? m->dm.lcap - lused : 0) + lfree;
   if (lavail < leaves) {
-    const int st = grow_leaf(m, std::max<size_t>(size_t(m->dm.lcap) * 2, lused + leaves));
+    const int st =
+        soft(grow_leaf(m, std::max<size_t>(size_t(m->dm.lcap) * 2, lused + leaves)));
     if (st) return st;
   }
   const size_t iused = m->h_ctr[C_INNER];
   if ((m->dm.icap > iused ? m->dm.icap - iused : 0) < inners) {
-    const int st = grow_inner(m, std::max<size_t>(size_t(m->dm.icap) * 2, iused + inners));
+    const int st =
+        soft(grow_inner(m, std::max<size_t>(size_t(m->dm.icap) * 2, iused + inners)));
     if (st) return st;
   }
   const size_t hcap = size_t(m->dm.hmask) + 1;
   if (m->h_ctr[C_ROOTS] + inners > m->load_factor * hcap) {
     size_t want = hcap * 2;
     while (m->h_ctr[C_ROOTS] + inners > m->load_factor * want) want *= 2;
-    const int st = grow_hash(m, want);
+    const int st = soft(grow_hash(m, want));
     if (st) return st;
   }
   return BXG_OK;
@@ -586,3 +603,176 @@ const char* bxg_last_error(const void* handle) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Serialization in the reference's format (serialization.hpp:77-116):
+//   "Bonxai::VoxelGrid<type,inner_bits,leaf_bits>(resolution)\n"
+//   uint32 root count; per root: int32 x, y, z; inner mask words; per inner
+//   bit set (ascending): leaf mask words, then each on cell's value
+//   (ascending cell index).
+// Roots are written in ascending (x, y, z) order (the reference writes them in
+// its unordered_map's order; any order deserializes to the same grid).
+// ---------------------------------------------------------------------------
+#include <map>
+#include <vector>
+
+namespace {
+
+struct HostImage {
+  std::vector<uint4> buckets;
+  std::vector<uint64_t> imask;
+  std::vector<uint32_t> ichild;
+  std::vector<uint64_t> lmask;
+  std::vector<uint8_t> ldata;
+};
+
+int download(bxg::MapCore* m, HostImage& im) {
+  using namespace bxg;
+  int st = core_sync(m);
+  if (st) return st;
+  const size_t hcap = size_t(m->dm.hmask) + 1;
+  const size_t ni = std::min<size_t>(m->h_ctr[C_INNER], m->dm.icap);
+  const size_t nl = std::min<size_t>(m->h_ctr[C_LEAF], m->dm.lcap);
+  im.buckets.resize(hcap);
+  im.imask.resize(ni * m->dm.iwords);
+  im.ichild.resize(ni * m->dm.isize);
+  im.lmask.resize(nl * m->dm.lwords);
+  im.ldata.resize(nl * m->dm.lsize * size_t(m->dm.esz));
+  BXG_CUDA(m, cudaMemcpy(im.buckets.data(), m->buckets.p, hcap * 16, cudaMemcpyDeviceToHost));
+  if (ni) {
+    BXG_CUDA(m, cudaMemcpy(im.imask.data(), m->imask.p, im.imask.size() * 8, cudaMemcpyDeviceToHost));
+    BXG_CUDA(m, cudaMemcpy(im.ichild.data(), m->ichild.p, im.ichild.size() * 4, cudaMemcpyDeviceToHost));
+  }
+  if (nl) {
+    BXG_CUDA(m, cudaMemcpy(im.lmask.data(), m->lmask.p, im.lmask.size() * 8, cudaMemcpyDeviceToHost));
+    if (!im.ldata.empty())
+      BXG_CUDA(m, cudaMemcpy(im.ldata.data(), m->ldata.p, im.ldata.size(), cudaMemcpyDeviceToHost));
+  }
+  return BXG_OK;
+}
+
+struct Writer {
+  uint8_t* out;
+  size_t cap, n = 0;
+  void put(const void* p, size_t k) {
+    if (out && n + k <= cap) std::memcpy(out + n, p, k);
+    n += k;
+  }
+};
+
+}  // namespace
+
+extern "C" int bxg_grid_serialize(bxg_grid g, const char* type_name, void* out, size_t cap,
+                                  size_t* n_out) {
+  if (!g || !type_name) return BXG_ERR_INVALID_ARG;
+  bxg::MapCore* m = const_cast<bxg::MapCore*>(bxg::core_of_handle(g));
+  cudaSetDevice(m->device);
+  HostImage im;
+  int st = download(m, im);
+  if (st) return st;
+  const bxg::DMap& d = m->dm;
+  std::map<std::array<int32_t, 3>, uint32_t> roots;  // sorted root key -> inner slot
+  for (const uint4& b : im.buckets) {
+    if (static_cast<int>(b.x) == bxg::kEmptyKey || b.w >= bxg::kPending) continue;
+    bool any = false;
+    for (int w = 0; w < d.iwords; w++) any |= im.imask[size_t(b.w) * d.iwords + w] != 0;
+    if (!any) continue;  // a root whose leaves were all released
+    roots[{int32_t(b.x), int32_t(b.y), int32_t(b.z)}] = b.w;
+  }
+  Writer wr{static_cast<uint8_t*>(out), cap};
+  char header[256];
+  std::snprintf(header, sizeof(header), "Bonxai::VoxelGrid<%s,%d,%d>(%lf)\n", type_name, d.ib,
+                d.lb, m->res);
+  wr.put(header, std::strlen(header));
+  const uint32_t nroots = uint32_t(roots.size());
+  wr.put(&nroots, 4);
+  for (const auto& kv : roots) {
+    wr.put(kv.first.data(), 12);
+    const uint32_t in = kv.second;
+    const uint64_t* im_w = im.imask.data() + size_t(in) * d.iwords;
+    wr.put(im_w, size_t(d.iwords) * 8);
+    for (int iw = 0; iw < d.iwords; iw++) {
+      for (uint64_t bits = im_w[iw]; bits; bits &= bits - 1) {
+        const uint32_t ii = uint32_t(iw * 64 + __builtin_ctzll(bits));
+        const uint32_t lf = im.ichild[size_t(in) * d.isize + ii];
+        const uint64_t* lm = im.lmask.data() + size_t(lf) * d.lwords;
+        wr.put(lm, size_t(d.lwords) * 8);
+        if (!d.esz) continue;
+        for (int lw = 0; lw < d.lwords; lw++)
+          for (uint64_t cb = lm[lw]; cb; cb &= cb - 1) {
+            const uint32_t ci = uint32_t(lw * 64 + __builtin_ctzll(cb));
+            wr.put(im.ldata.data() + (size_t(lf) * d.lsize + ci) * d.esz, size_t(d.esz));
+          }
+      }
+    }
+  }
+  if (n_out) *n_out = wr.n;
+  if (out && wr.n > cap) return bxg::set_error(m, BXG_ERR_CAPACITY, "output buffer too small");
+  return BXG_OK;
+}
+
+extern "C" int bxg_grid_deserialize(bxg_grid g, const void* data, size_t n) {
+  if (!g || !data) return BXG_ERR_INVALID_ARG;
+  bxg::MapCore* m = const_cast<bxg::MapCore*>(bxg::core_of_handle(g));
+  const bxg::DMap& d = m->dm;
+  const uint8_t* p = static_cast<const uint8_t*>(data);
+  const uint8_t* end = p + n;
+  // header line (serialization.hpp:126-151): prefix, type, bits, resolution
+  const uint8_t* nl = static_cast<const uint8_t*>(std::memchr(p, '\n', n));
+  if (!nl) return bxg::set_error(m, BXG_ERR_INVALID_ARG, "Header wasn't recognized");
+  const std::string header(reinterpret_cast<const char*>(p), nl - p);
+  if (header.rfind("Bonxai::VoxelGrid<", 0) != 0)
+    return bxg::set_error(m, BXG_ERR_INVALID_ARG, "Header wasn't recognized");
+  const size_t lt = header.rfind('>');
+  const size_t c2 = header.rfind(',', lt);
+  const size_t c1 = header.rfind(',', c2 - 1);
+  if (lt == std::string::npos || c1 == std::string::npos || c2 == std::string::npos)
+    return bxg::set_error(m, BXG_ERR_INVALID_ARG, "Header wasn't recognized");
+  const int ib = std::atoi(header.substr(c1 + 1, c2 - c1 - 1).c_str());
+  const int lb = std::atoi(header.substr(c2 + 1, lt - c2 - 1).c_str());
+  if (ib != d.ib || lb != d.lb)
+    return bxg::set_error(m, BXG_ERR_INVALID_ARG, "inner/leaf bits do not match this grid");
+  p = nl + 1;
+  auto take = [&](void* dst, size_t k) -> bool {
+    if (size_t(end - p) < k) return false;
+    std::memcpy(dst, p, k);
+    p += k;
+    return true;
+  };
+  uint32_t nroots = 0;
+  if (!take(&nroots, 4)) return bxg::set_error(m, BXG_ERR_INVALID_ARG, "truncated stream");
+  std::vector<int32_t> xyz;
+  std::vector<uint8_t> vals;
+  std::vector<uint64_t> iw(d.iwords), lw(d.lwords);
+  const int im = (1 << d.ib) - 1, lm = (1 << d.lb) - 1;
+  for (uint32_t r = 0; r < nroots; r++) {
+    int32_t key[3];
+    if (!take(key, 12) || !take(iw.data(), iw.size() * 8))
+      return bxg::set_error(m, BXG_ERR_INVALID_ARG, "truncated stream");
+    for (int a = 0; a < d.iwords; a++)
+      for (uint64_t bits = iw[a]; bits; bits &= bits - 1) {
+        const int ii = a * 64 + __builtin_ctzll(bits);
+        const int xb = key[0] | ((ii & im) << d.lb), yb = key[1] | (((ii >> d.ib) & im) << d.lb),
+                  zb = key[2] | (((ii >> (2 * d.ib)) & im) << d.lb);
+        if (!take(lw.data(), lw.size() * 8))
+          return bxg::set_error(m, BXG_ERR_INVALID_ARG, "truncated stream");
+        for (int b = 0; b < d.lwords; b++)
+          for (uint64_t cb = lw[b]; cb; cb &= cb - 1) {
+            const int ci = b * 64 + __builtin_ctzll(cb);
+            xyz.push_back(xb | (ci & lm));
+            xyz.push_back(yb | ((ci >> d.lb) & lm));
+            xyz.push_back(zb | ((ci >> (2 * d.lb)) & lm));
+            if (d.esz) {
+              const size_t off = vals.size();
+              vals.resize(off + d.esz);
+              if (!take(vals.data() + off, d.esz))
+                return bxg::set_error(m, BXG_ERR_INVALID_ARG, "truncated stream");
+            }
+          }
+      }
+  }
+  const size_t cells = xyz.size() / 3;
+  if (!cells) return BXG_OK;
+  if (d.esz) return bxg_grid_set_values(g, xyz.data(), vals.data(), cells, nullptr);
+  return bxg_grid_set_cells_on(g, xyz.data(), cells, nullptr, nullptr);
+}

@@ -706,6 +706,24 @@ int bxg_grid_synchronize(bxg_grid g) {
   return core_sync(&g->core);
 }
 
+int bxg_grid_device_view(bxg_grid g, bxg_device_view* out) {
+  if (check_grid(g) || !out) return BXG_ERR_INVALID_ARG;
+  MapCore* m = &g->core;
+  cudaSetDevice(m->device);
+  const int st = core_sync(m);
+  if (st) return st;
+  out->leaf_mask = m->dm.lmask;
+  out->leaf_data = m->dm.ldata;
+  out->leaf_key = reinterpret_cast<const int32_t*>(m->dm.lkey);
+  out->n_leaves = m->h_ctr[C_LEAF];
+  out->inner_bits = m->dm.ib;
+  out->leaf_bits = m->dm.lb;
+  out->value_bytes = m->dm.esz;
+  out->resolution = m->res;
+  out->stream = m->stream;
+  return BXG_OK;
+}
+
 }  // extern "C"
 
 // ---------------------------------------------------------------------------

@@ -40,6 +40,41 @@ __global__ void k_endpoints(DMap M, const uint8_t* __restrict__ pts, size_t stri
   if (e.w != EP_SKIP) dedup_min_insert(tab, tmask, e.x, e.y, e.z, i, M);
 }
 
+// A sensor-frame cloud with its sensor-to-world transform (row-major 3x4),
+// the ingest of bonxai_ros/src/bonxai_server.cpp:147-171 fused into the
+// endpoint kernel: points with a non-finite coordinate are dropped (:147-154),
+// the rest are transformed in float (:166-168), then handled as k_endpoints
+// does. A dropped point keeps its index, so the lowest-index rule gives the
+// same winners as the host's compaction. Transform order per axis, in float
+// without contraction: ((m[r][0]*x + m[r][1]*y) + m[r][2]*z) + m[r][3].
+struct Xf {
+  float m[12];
+};
+
+__device__ __forceinline__ float xf_row(const Xf& t, int r, float x, float y, float z) {
+  return __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(t.m[4 * r], x), __fmul_rn(t.m[4 * r + 1], y)),
+                             __fmul_rn(t.m[4 * r + 2], z)),
+                   t.m[4 * r + 3]);
+}
+
+__global__ void k_endpoints_sensor(DMap M, const uint8_t* __restrict__ pts, size_t stride,
+                                   uint32_t n, Xf xf, double fx, double fy, double fz,
+                                   double max_range, double mr2, double inv_res,
+                                   int4* __restrict__ ep, uint4* tab, uint32_t tmask) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float* p = reinterpret_cast<const float*>(pts + size_t(i) * stride);
+  const float x = p[0], y = p[1], z = p[2];
+  if (!(isfinite(x) && isfinite(y) && isfinite(z))) {
+    ep[i] = make_int4(0, 0, 0, EP_SKIP);
+    return;
+  }
+  const float w[3] = {xf_row(xf, 0, x, y, z), xf_row(xf, 1, x, y, z), xf_row(xf, 2, x, y, z)};
+  const int4 e = compute_endpoint<float>(w, fx, fy, fz, max_range, mr2, inv_res, true);
+  ep[i] = e;
+  if (e.w != EP_SKIP) dedup_min_insert(tab, tmask, e.x, e.y, e.z, i, M);
+}
+
 // addHitPoint / addMissPoint batches: double points with a given kind, or a
 // per-point kind (0 hit, 1 miss) when kinds != nullptr.
 __global__ void k_endpoints_kind(DMap M, const double* __restrict__ pts, uint32_t n, int kind,
@@ -114,10 +149,14 @@ __global__ void k_apply(DMap M, const int4* __restrict__ cast, uint32_t cast_cap
 
 // Ray phase: one group of W lanes per listed ray (walk_ray, or walk_ray2 with
 // two cells per lane per step when U == 2).
-template <int W, int U>
+// CHUNK: each group takes a contiguous run of the ray list instead of every
+// ngroups-th ray (neighbouring rays share leaves). CACHE (W = 32, U = 1): a
+// per-warp leaf cache in shared memory (walk_ray_op).
+template <int W, int U, bool CHUNK = false, bool CACHE = false>
 __global__ void __launch_bounds__(256, U == 2 ? 3 : 4) k_rays(DMap M, const int4* __restrict__ cast,
                                                  uint32_t cast_cap, int ox, int oy, int oz,
                                                  int32_t u, int32_t miss, int32_t cmin) {
+  extern __shared__ uint4 k_rays_smem[];
   const uint32_t n_cast = min(ld_volatile(M.ctr + C_CAST), cast_cap);
   const unsigned lane = threadIdx.x & 31;
   const unsigned sl = lane & (W - 1);
@@ -125,12 +164,25 @@ __global__ void __launch_bounds__(256, U == 2 ? 3 : 4) k_rays(DMap M, const int4
   const unsigned gmask = (W == 32) ? 0xffffffffu : (((1u << W) - 1u) << gbase);
   const uint32_t gid = (blockIdx.x * blockDim.x + threadIdx.x) / W;
   const uint32_t ngroups = (gridDim.x * blockDim.x) / W;
+  uint4* lc = nullptr;
+  if (CACHE) {
+    lc = k_rays_smem + (threadIdx.x / 32) * kLeafCache;
+    for (int i = lane; i < kLeafCache; i += 32) lc[i] = make_uint4(kNone, kNone, kNone, kNone);
+    __syncwarp();
+  }
+  uint32_t r = gid, r_end = n_cast, r_step = ngroups;
+  if (CHUNK) {
+    const uint32_t chunk = (n_cast + ngroups - 1) / ngroups;
+    r = min(gid * chunk, n_cast);
+    r_end = min(r + chunk, n_cast);
+    r_step = 1;
+  }
   uint32_t visited = 0, updated = 0;
-  for (uint32_t r = gid; r < n_cast; r += ngroups) {
+  for (; r < r_end; r += r_step) {
     if (U == 2)
       walk_ray2<W>(M, cast[r], ox, oy, oz, u, miss, cmin, sl, gbase, gmask, visited, updated);
     else
-      walk_ray<W>(M, cast[r], ox, oy, oz, u, miss, cmin, sl, gbase, gmask, visited, updated);
+      walk_ray<W>(M, cast[r], ox, oy, oz, u, miss, cmin, sl, gbase, gmask, visited, updated, lc);
   }
   visited = __reduce_add_sync(0xffffffffu, visited);
   updated = __reduce_add_sync(0xffffffffu, updated);
@@ -281,6 +333,18 @@ int launch_rays(bxg_pmap_s* pm, int ox, int oy, int oz) {
   const dim3 g{unsigned(blocks)}, b{unsigned(bs)};
   const int4* c = m->s_cast.as<int4>();
   const int32_t uc = pm->update_count;
+  const bool chunk = m->flags & BXG_FLAG_RAY_CHUNKS, cache = m->flags & BXG_FLAG_LEAF_CACHE;
+  if (rpw == 1 && !u2 && (chunk || cache)) {
+    const size_t smem = cache ? size_t(bs / 32) * kLeafCache * sizeof(uint4) : 0;
+    if (chunk && cache)
+      k_rays<32, 1, true, true><<<g, b, smem, m->stream>>>(m->dm, c, ccap, ox, oy, oz, uc, o.miss, o.cmin);
+    else if (chunk)
+      k_rays<32, 1, true, false><<<g, b, 0, m->stream>>>(m->dm, c, ccap, ox, oy, oz, uc, o.miss, o.cmin);
+    else
+      k_rays<32, 1, false, true><<<g, b, smem, m->stream>>>(m->dm, c, ccap, ox, oy, oz, uc, o.miss, o.cmin);
+    BXG_LAUNCHED(m);
+    return BXG_OK;
+  }
   if (rpw == 4) {
     if (u2) k_rays<8, 2><<<g, b, 0, m->stream>>>(m->dm, c, ccap, ox, oy, oz, uc, o.miss, o.cmin);
     else k_rays<8, 1><<<g, b, 0, m->stream>>>(m->dm, c, ccap, ox, oy, oz, uc, o.miss, o.cmin);
@@ -359,7 +423,7 @@ int origin_coord(const MapCore* m, double x, double y, double z, int* c) {
 
 template <typename PT>
 int insert_impl(bxg_pmap m_, const PT* xyz, size_t stride, size_t n, const PT* origin,
-                double max_range, uint64_t* ray_cells, bool sync) {
+                double max_range, uint64_t* ray_cells, bool sync, const Xf* xf = nullptr) {
   if (!m_) return BXG_ERR_INVALID_ARG;
   bxg_pmap_s* pm = m_;
   MapCore* m = &pm->core;
@@ -389,9 +453,14 @@ int insert_impl(bxg_pmap m_, const PT* xyz, size_t stride, size_t n, const PT* o
     const int keep = (m->flags & BXG_FLAG_KEEP_NONFINITE) ? 1 : 0;
     st = endpoint_phase(pm, uint32_t(n), o[0], o[1], o[2],
                         [&](unsigned blocks, int4* ep, uint4* tab, uint32_t tmask) {
-                          k_endpoints<PT><<<blocks, 256, 0, m->stream>>>(
-                              m->dm, static_cast<const uint8_t*>(dpts), stride, uint32_t(n), fx,
-                              fy, fz, max_range, mr2, m->inv_res, keep, ep, tab, tmask);
+                          if (xf)
+                            k_endpoints_sensor<<<blocks, 256, 0, m->stream>>>(
+                                m->dm, static_cast<const uint8_t*>(dpts), stride, uint32_t(n),
+                                *xf, fx, fy, fz, max_range, mr2, m->inv_res, ep, tab, tmask);
+                          else
+                            k_endpoints<PT><<<blocks, 256, 0, m->stream>>>(
+                                m->dm, static_cast<const uint8_t*>(dpts), stride, uint32_t(n), fx,
+                                fy, fz, max_range, mr2, m->inv_res, keep, ep, tab, tmask);
                         });
     if (st) return st;
   }
@@ -440,6 +509,97 @@ int add_points(bxg_pmap m_, const double* xyz, size_t n, int kind,
   if (st) return st;
   // apply now so that queries see the endpoint updates, as in the reference
   return finish_scan(pm, 0, 0, 0, false, nullptr, false);
+}
+
+// The occupied-voxel export of bonxai_server.cpp:217-243 as one compaction:
+// each occupied cell (probability_log > thr, probabilistic_map.cpp:108-116)
+// becomes its corner position coordToPos(c) = double(c) * res
+// (bonxai.hpp:413-417), kept when min_z <= z <= max_z, narrowed to float
+// xyz (the PCLPoint the node publishes). One thread per leaf mask word; a
+// warp reserves its output range with one atomic. Order is unspecified, as
+// the reference's unordered_map order is.
+__global__ void k_export_occupied(DMap M, uint32_t n_leaves, float* __restrict__ out, size_t cap,
+                                  unsigned long long* __restrict__ counter, int32_t thr,
+                                  double res, double min_z, double max_z) {
+  const size_t t = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+  const uint32_t leaf = static_cast<uint32_t>(t / M.lwords);
+  const uint32_t wi = static_cast<uint32_t>(t % M.lwords);
+  const int lm = (1 << M.lb) - 1;
+  unsigned long long w = 0;
+  int4 key = make_int4(0, 0, 0, -1);
+  if (leaf < n_leaves) {
+    key = M.lkey[leaf];
+    if (key.w != -1) w = M.lmask[static_cast<size_t>(leaf) * M.lwords + wi];
+  }
+  if (w) {
+    const int32_t* cells = reinterpret_cast<const int32_t*>(M.ldata) +
+                           static_cast<size_t>(leaf) * M.lsize + wi * 64;
+    unsigned long long f = 0, rest = w;
+    while (rest) {
+      const int b = __ffsll(static_cast<long long>(rest)) - 1;
+      rest &= rest - 1;
+      const uint32_t ci = wi * 64 + b;
+      const double pz = __dmul_rn(double(key.z | int((ci >> (2 * M.lb)) & lm)), res);
+      if (cell_prob(cells[b]) > thr && pz >= min_z && pz <= max_z) f |= 1ull << b;
+    }
+    w = f;
+  }
+  const unsigned cnt = __popcll(w);
+  const unsigned lane = threadIdx.x & 31;
+  unsigned incl = cnt;
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned v = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= static_cast<unsigned>(o)) incl += v;
+  }
+  const unsigned total = __shfl_sync(0xffffffffu, incl, 31);
+  unsigned long long base = 0;
+  if (lane == 31 && total) base = atomicAdd(counter, static_cast<unsigned long long>(total));
+  base = __shfl_sync(0xffffffffu, base, 31);
+  unsigned long long pos = base + incl - cnt;
+  while (w) {
+    const int b = __ffsll(static_cast<long long>(w)) - 1;
+    w &= w - 1;
+    const uint32_t ci = wi * 64 + b;
+    if (pos < cap) {
+      out[3 * pos + 0] = float(__dmul_rn(double(key.x | int(ci & lm)), res));
+      out[3 * pos + 1] = float(__dmul_rn(double(key.y | int((ci >> M.lb) & lm)), res));
+      out[3 * pos + 2] = float(__dmul_rn(double(key.z | int((ci >> (2 * M.lb)) & lm)), res));
+    }
+    pos++;
+  }
+}
+
+int export_occupied(bxg_pmap m_, float* out_xyz, size_t cap, size_t* n_out, double min_z,
+                    double max_z) {
+  MapCore* m = &m_->core;
+  int st = core_sync(m);
+  if (st) return st;
+  const uint32_t n_leaves = m->h_ctr[C_LEAF];
+  void* dout = nullptr;
+  if (cap && out_xyz) {
+    st = stage_out(m, m->s_out, out_xyz, cap * 12, &dout);
+    if (st) return st;
+  }
+  BXG_CUDA(m, m->s_tmp.ensure(8));
+  BXG_CUDA(m, cudaMemsetAsync(m->s_tmp.p, 0, 8, m->stream));
+  const size_t threads = size_t(n_leaves) * m->dm.lwords;
+  const size_t wcap = dout ? cap : 0;
+  if (threads) {
+    k_export_occupied<<<unsigned((threads + 255) / 256), 256, 0, m->stream>>>(
+        m->dm, n_leaves, static_cast<float*>(dout), wcap, m->s_tmp.as<unsigned long long>(),
+        m_->opt.occupancy_threshold_log, m->res, min_z, max_z);
+    BXG_LAUNCHED(m);
+  }
+  unsigned long long n = 0;
+  BXG_CUDA(m, cudaMemcpyAsync(&n, m->s_tmp.p, 8, cudaMemcpyDeviceToHost, m->stream));
+  BXG_CUDA(m, cudaStreamSynchronize(m->stream));
+  if (dout) {
+    st = stage_out_finish(m, out_xyz, dout, std::min<size_t>(size_t(n), wcap) * 12);
+    if (st) return st;
+  }
+  if (n_out) *n_out = size_t(n);
+  if (size_t(n) > cap) return set_error(m, BXG_ERR_CAPACITY, "output buffer too small");
+  return BXG_OK;
 }
 
 int query(bxg_pmap m_, const int32_t* xyz, size_t n, uint8_t* out, int mode) {
@@ -558,6 +718,26 @@ int bxg_pmap_insert_point_cloud_f64(bxg_pmap m, const double* xyz, size_t stride
 int bxg_pmap_insert_point_cloud_f32_async(bxg_pmap m, const float* xyz, size_t stride,
                                           size_t n, const float origin[3], double max_range) {
   return insert_impl(m, xyz, stride, n, origin, max_range, nullptr, false);
+}
+
+int bxg_pmap_insert_sensor_cloud_f32(bxg_pmap m, const float* xyz, size_t stride, size_t n,
+                                     const float sensor_to_world[12], double max_range,
+                                     uint64_t* ray_cells) {
+  if (!m || !sensor_to_world) return BXG_ERR_INVALID_ARG;
+  Xf xf;
+  std::memcpy(xf.m, sensor_to_world, sizeof(xf.m));
+  // origin = the transform's translation (bonxai_server.cpp:171-173); a
+  // negative max_range means no limit (:174-179)
+  const float origin[3] = {xf.m[3], xf.m[7], xf.m[11]};
+  if (max_range < 0) max_range = HUGE_VAL;
+  return insert_impl(m, xyz, stride, n, origin, max_range, ray_cells, true, &xf);
+}
+
+int bxg_pmap_export_occupied_f32(bxg_pmap m, float* out_xyz, size_t cap, size_t* n_out,
+                                 double min_z, double max_z) {
+  if (!m) return BXG_ERR_INVALID_ARG;
+  cudaSetDevice(m->core.device);
+  return export_occupied(m, out_xyz, cap, n_out, min_z, max_z);
 }
 
 int bxg_pmap_add_hit_points(bxg_pmap m, const double* xyz, size_t n) {

@@ -73,6 +73,11 @@ typedef struct {
 #define BXG_FLAG_TIMING 2u
 /* Batched ticks: launch directly instead of replaying a captured CUDA graph. */
 #define BXG_FLAG_NO_GRAPH 4u
+/* Per-map ray kernel shape (rays_per_warp 1, ray_unroll 1): each warp walks a
+ * contiguous run of the ray list; and/or keeps a leaf-slot cache in shared
+ * memory. Same results. */
+#define BXG_FLAG_RAY_CHUNKS 8u
+#define BXG_FLAG_LEAF_CACHE 16u
 
 void bxg_config_default(bxg_config* cfg);
 const char* bxg_status_string(int status);
@@ -159,6 +164,36 @@ int bxg_grid_clear(bxg_grid g, int option);
  * back to the pool, and roots with no leaf leave the root map. */
 int bxg_grid_release_unused(bxg_grid g);
 int bxg_grid_synchronize(bxg_grid g);
+/* The grid's leaf pool as raw device pointers, for device-side visitors
+ * (include/bonxai/device_visit.cuh): leaf l holds mask words
+ * leaf_mask[l * words .. + words) (words = max(8^leaf_bits / 64, 1)), cell
+ * values leaf_data[(l * 8^leaf_bits + i) * value_bytes] with i = x | y << lb |
+ * z << 2lb (bonxai.hpp:441-447), and its corner coordinate
+ * leaf_key[4l .. 4l+2] (leaf_key[4l+3] == -1: a free slot). Valid until the
+ * next call that can grow the pools. Synchronises the grid's stream. */
+typedef struct {
+  unsigned long long* leaf_mask;
+  unsigned char* leaf_data;
+  const int32_t* leaf_key;
+  uint32_t n_leaves;
+  int inner_bits, leaf_bits;
+  int value_bytes;
+  double resolution;
+  void* stream; /* cudaStream_t the grid runs on */
+} bxg_device_view;
+int bxg_grid_device_view(bxg_grid g, bxg_device_view* out);
+
+/* Serialize(out, grid) (bonxai_core/include/bonxai/serialization.hpp:77-116):
+ * the reference's byte format -- header line
+ * "Bonxai::VoxelGrid<type_name,inner_bits,leaf_bits>(resolution)\n", uint32
+ * root count, per root its key, inner mask words, and per leaf its mask words
+ * and on-cell values -- with roots in ascending key order. type_name is the
+ * demangled C++ type (e.g. "float"). Two-call pattern: *n_out = bytes needed;
+ * BXG_ERR_CAPACITY if cap was too small. */
+int bxg_grid_serialize(bxg_grid g, const char* type_name, void* out, size_t cap, size_t* n_out);
+/* Deserialize (serialization.hpp:126-199) into this grid (its bits must match
+ * the header's; values are set like setValue). */
+int bxg_grid_deserialize(bxg_grid g, const void* data, size_t n);
 
 /* ========================================================================
  * ProbabilisticMap  (bonxai_map/include/bonxai_map/probabilistic_map.hpp:27-137)
@@ -205,6 +240,18 @@ int bxg_pmap_add_points(bxg_pmap m, const double* xyz, const uint8_t* kinds, siz
 int bxg_pmap_insert_point_cloud_f32_async(bxg_pmap m, const float* xyz, size_t stride,
                                           size_t n, const float origin[3], double max_range);
 
+/* The ROS node's cloud callback (bonxai_ros/src/bonxai_server.cpp:140-182)
+ * fused into one scan: n float x,y,z points in the SENSOR frame (byte stride,
+ * 0 = packed), sensor_to_world a row-major 3x4 float transform [R | t].
+ * Points with a non-finite coordinate are dropped (:147-154); the others are
+ * transformed in float, ((r0*x + r1*y) + r2*z) + t per axis without
+ * contraction (pcl::transformPointCloud, :166-168), and inserted from the
+ * origin t (:171-173) as bxg_pmap_insert_point_cloud_f32 would; max_range < 0
+ * means no limit (:174-179). */
+int bxg_pmap_insert_sensor_cloud_f32(bxg_pmap m, const float* xyz, size_t stride, size_t n,
+                                     const float sensor_to_world[12], double max_range,
+                                     uint64_t* ray_cells);
+
 /* addHitPoint / addMissPoint for n double points, in order
  * (probabilistic_map.hpp:98,103, probabilistic_map.cpp:30-54). The cells are
  * updated immediately; their rays are cast by bxg_pmap_update_free_cells. */
@@ -223,6 +270,14 @@ int bxg_pmap_is_free(bxg_pmap m, const int32_t* xyz, size_t n, uint8_t* out);
 /* getOccupiedVoxels / getFreeVoxels (probabilistic_map.cpp:108-126), unordered. */
 int bxg_pmap_get_occupied(bxg_pmap m, int32_t* out_xyz, size_t cap, size_t* n_out);
 int bxg_pmap_get_free(bxg_pmap m, int32_t* out_xyz, size_t cap, size_t* n_out);
+/* The occupied-voxel export of the ROS node (bonxai_server.cpp:217-243): the
+ * PointT overload of getOccupiedVoxels (probabilistic_map.hpp:115-124), i.e.
+ * corner positions double(c) * resolution, kept where min_z <= z <= max_z,
+ * written as float x,y,z. out_xyz may be device memory (a headless buffer
+ * that stays on the GPU) or host memory. Unordered; BXG_ERR_CAPACITY with
+ * *n_out set when cap is too small. */
+int bxg_pmap_export_occupied_f32(bxg_pmap m, float* out_xyz, size_t cap, size_t* n_out,
+                                 double min_z, double max_z);
 /* grid().forEachCell over the map (bonxai.hpp:703-743): coordinates and the
  * packed 4-byte CellT words (update_id in bits 0-3, probability_log in bits
  * 4-31, the layout GCC gives probabilistic_map.hpp:44-53). */

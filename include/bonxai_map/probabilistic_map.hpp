@@ -156,6 +156,36 @@ class ProbabilisticMap {
         bxg_pmap_insert_point_cloud_f32(h_, xyz, 0, n, origin, max_range, &last_ray_cells_), h_);
   }
 
+  /// The ROS node's cloud callback (bonxai_server.cpp:140-182) as one scan:
+  /// float points in the sensor frame and the sensor-to-world transform as
+  /// any 4x4 or 3x4 matrix type with operator()(row, col) (Eigen::Matrix4f
+  /// works). Non-finite points are dropped, the rest transformed in float on
+  /// the GPU, the origin is the translation, max_range < 0 means no limit.
+  template <typename PointT, typename Allocator, typename Matrix>
+  void insertSensorCloud(const std::vector<PointT, Allocator>& sensor_points,
+                         const Matrix& sensor_to_world, double max_range) {
+    std::vector<float> xyz(sensor_points.size() * 3);
+    for (size_t i = 0; i < sensor_points.size(); i++) {
+      const auto p = ConvertPoint<Point3D>(sensor_points[i]);
+      xyz[3 * i] = float(p.x);
+      xyz[3 * i + 1] = float(p.y);
+      xyz[3 * i + 2] = float(p.z);
+    }
+    float m[12];
+    for (int r = 0; r < 3; r++)
+      for (int c = 0; c < 4; c++) m[4 * r + c] = float(sensor_to_world(r, c));
+    insertSensorCloud(xyz.data(), sensor_points.size(), m, max_range);
+  }
+  /// Batch form: n packed float xyz points (host or device memory) and a
+  /// row-major 3x4 transform.
+  void insertSensorCloud(const float* xyz, size_t n, const float sensor_to_world[12],
+                         double max_range) {
+    flush();
+    detail::check(bxg_pmap_insert_sensor_cloud_f32(h_, xyz, 0, n, sensor_to_world, max_range,
+                                                   &last_ray_cells_),
+                  h_);
+  }
+
   /// addHitPoint / addMissPoint (probabilistic_map.hpp:95-103).
   template <typename V>
   void addHitPoint(const V& point) {
@@ -201,6 +231,25 @@ class ProbabilisticMap {
       const auto p = grid_.coordToPos(c);
       points.emplace_back(p.x, p.y, p.z);
     }
+  }
+
+  /// The ROS node's occupied-voxel export (bonxai_server.cpp:217-243) on the
+  /// GPU: corner positions of occupied cells with min_z <= z <= max_z as
+  /// float xyz into out_xyz (host or device memory, cap points). Returns the
+  /// number of such cells; throws if it exceeds cap.
+  size_t exportOccupied(float* out_xyz, size_t cap, double min_z, double max_z) {
+    flush();
+    size_t n = 0;
+    detail::check(bxg_pmap_export_occupied_f32(h_, out_xyz, cap, &n, min_z, max_z), h_);
+    return n;
+  }
+  /// Number of occupied cells in the z band (no output written).
+  size_t countOccupied(double min_z, double max_z) {
+    flush();
+    size_t n = 0;
+    const int st = bxg_pmap_export_occupied_f32(h_, nullptr, 0, &n, min_z, max_z);
+    if (st != BXG_OK && st != BXG_ERR_CAPACITY) detail::check(st, h_);
+    return n;
   }
 
   /// Ray-cell updates of the last insertPointCloud (points + ray cells) or

@@ -112,6 +112,8 @@ class Grid {
       : ib_(ib), lb_(lb), res_(res), inv_res_(1.0 / res),  // bonxai.hpp:390-398
         inner_mask_((1 << ib) - 1), leaf_mask_((1 << lb) - 1) {}
 
+  double resolution() const { return res_; }
+
   // posToCoord: floor(x * inv_resolution) in double (bonxai.hpp:404-410).
   Coord pos_to_coord(double x, double y, double z) const {
     return {int32_t(std::floor(x * inv_res_)), int32_t(std::floor(y * inv_res_)),
@@ -603,6 +605,28 @@ static size_t pmap_filter(void* m, int32_t* xyz, size_t cap, int sign) {
 size_t orc_pmap_get_occupied(void* m, int32_t* xyz, size_t cap) {
   return pmap_filter(m, xyz, cap, 1);
 }
+// The ROS node's occupied-voxel export (bonxai_server.cpp:217-243): the
+// PointT getOccupiedVoxels (probabilistic_map.hpp:115-124) gives corner
+// positions double(c) * resolution (bonxai.hpp:413-417); z in [min_z, max_z]
+// is kept and narrowed to float.
+size_t orc_pmap_export_occupied_f32(void* m, double min_z, double max_z, float* xyz,
+                                    size_t cap) {
+  auto* p = static_cast<orc::PMap*>(m);
+  const double res = p->grid().resolution();
+  size_t k = 0;
+  p->grid().for_each([&](const int32_t& w, const Coord& c) {
+    if (!(orc::cell_prob(w) > p->thr)) return;
+    const double x = double(c.x) * res, y = double(c.y) * res, z = double(c.z) * res;
+    if (!(z >= min_z && z <= max_z)) return;
+    if (k < cap) {
+      xyz[3 * k] = float(x);
+      xyz[3 * k + 1] = float(y);
+      xyz[3 * k + 2] = float(z);
+    }
+    k++;
+  });
+  return k;
+}
 size_t orc_pmap_get_free(void* m, int32_t* xyz, size_t cap) {
   return pmap_filter(m, xyz, cap, -1);
 }
@@ -644,6 +668,27 @@ size_t orc_grid_dump(void* g, int32_t* xyz, void* v, size_t cap) {
 }
 void orc_grid_clear(void* g, int opt) { static_cast<orc::GridIf*>(g)->clear(opt); }
 void orc_grid_release_unused(void* g) { static_cast<orc::GridIf*>(g)->release(); }
+
+// The ROS node's cloud ingest (bonxai_server.cpp:147-168): drop points with a
+// non-finite coordinate, then transform by a row-major 3x4 float [R | t] in
+// float, ((r0*x + r1*y) + r2*z) + t per axis (built without contraction).
+// PCL is not part of the reference's repository; this operation order is the
+// stated assumption the GPU path shares. Returns the points kept.
+size_t orc_sensor_to_world_f32(const float* m12, const float* xyz, size_t n, float* out) {
+  size_t k = 0;
+  for (size_t i = 0; i < n; i++) {
+    const float x = xyz[3 * i], y = xyz[3 * i + 1], z = xyz[3 * i + 2];
+    if (!(std::isfinite(x) && std::isfinite(y) && std::isfinite(z))) continue;
+    for (int r = 0; r < 3; r++) {
+      float v = m12[4 * r] * x;
+      v = v + m12[4 * r + 1] * y;
+      v = v + m12[4 * r + 2] * z;
+      out[3 * k + r] = v + m12[4 * r + 3];
+    }
+    k++;
+  }
+  return k;
+}
 
 size_t orc_compute_ray(const int32_t* o, const int32_t* e, int32_t* out, size_t cap) {
   size_t k = 0;

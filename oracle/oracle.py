@@ -100,9 +100,19 @@ class OracleLib:
         for name, (res, args) in sig.items():
             f = getattr(L, name)
             f.restype, f.argtypes = res, args
+        if hasattr(L, "orc_pmap_export_occupied_f32"):
+            f = L.orc_pmap_export_occupied_f32
+            f.restype, f.argtypes = _sz, [_vp, _dbl, _dbl, _vp, _sz]
+        if hasattr(L, "orc_sensor_to_world_f32"):
+            f = L.orc_sensor_to_world_f32
+            f.restype, f.argtypes = _sz, [_vp, _vp, _sz, _vp]
         if hasattr(L, "orc_ref_insert_point_cloud_f32"):
             f = L.orc_ref_insert_point_cloud_f32
             f.restype, f.argtypes = None, [_vp, _vp, _sz, _vp, _dbl]
+        for name in ("orc_ref_grid_serialize", "orc_ref_pmap_serialize"):
+            if hasattr(L, name):
+                f = getattr(L, name)
+                f.restype, f.argtypes = _sz, [_vp, _vp, _sz]
 
     # ------------------------------------------------------------------ rays
     def compute_ray(self, o, e) -> np.ndarray:
@@ -112,6 +122,14 @@ class OracleLib:
         out = np.zeros((n, 3), np.int32)
         self.lib.orc_compute_ray(_ptr(o), _ptr(e), _ptr(out), n)
         return out
+
+    def sensor_to_world(self, m12, xyz) -> np.ndarray:
+        """The ROS node's ingest restated: finite points, transformed in float."""
+        m = np.ascontiguousarray(m12, np.float32).reshape(12)
+        p = np.ascontiguousarray(xyz, np.float32).reshape(-1, 3)
+        out = np.zeros_like(p)
+        k = self.lib.orc_sensor_to_world_f32(_ptr(m), _ptr(p), len(p), _ptr(out))
+        return out[:k]
 
     def pmap(self, resolution: float) -> "OraclePMap":
         return OraclePMap(self, resolution)
@@ -205,6 +223,21 @@ class OraclePMap:
     def occupied(self):
         return self._coords(self.lib.orc_pmap_get_occupied)
 
+    def export_occupied(self, min_z=-np.inf, max_z=np.inf) -> np.ndarray:
+        """Occupied corner positions as float xyz in the z band, sorted."""
+        fn = self.lib.orc_pmap_export_occupied_f32
+        n = fn(self.h, float(min_z), float(max_z), None, 0)
+        out = np.zeros((n, 3), np.float32)
+        fn(self.h, float(min_z), float(max_z), _ptr(out), n)
+        return out[np.lexsort((out[:, 2], out[:, 1], out[:, 0]))]
+
+    def serialize_reference(self) -> bytes:
+        """Bonxai::Serialize of the map's grid (reference library only)."""
+        n = self.lib.orc_ref_pmap_serialize(self.h, None, 0)
+        buf = C.create_string_buffer(n)
+        self.lib.orc_ref_pmap_serialize(self.h, buf, n)
+        return buf.raw[:n]
+
     def free(self):
         return self._coords(self.lib.orc_pmap_get_free)
 
@@ -282,6 +315,13 @@ class OracleGrid:
 
     def release_unused(self):
         self.lib.orc_grid_release_unused(self.h)
+
+    def serialize_reference(self) -> bytes:
+        """Bonxai::Serialize of this grid (reference library only)."""
+        n = self.lib.orc_ref_grid_serialize(self.h, None, 0)
+        buf = C.create_string_buffer(n)
+        self.lib.orc_ref_grid_serialize(self.h, buf, n)
+        return buf.raw[:n]
 
 
 _port = None

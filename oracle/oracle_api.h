@@ -51,6 +51,15 @@ void orc_pmap_query(void* m, const int32_t* xyz, size_t n, uint8_t* occ, uint8_t
                     uint8_t* fre);
 size_t orc_pmap_get_occupied(void* m, int32_t* xyz, size_t cap);
 size_t orc_pmap_get_free(void* m, int32_t* xyz, size_t cap);
+/* getOccupiedVoxels(std::vector<PointT>&) (probabilistic_map.hpp:115-124)
+ * filtered to min_z <= z <= max_z and narrowed to float, as the ROS node
+ * publishes it (bonxai_server.cpp:217-243). Any order; returns the count. */
+size_t orc_pmap_export_occupied_f32(void* m, double min_z, double max_z, float* xyz,
+                                    size_t cap);
+/* Restatement of the ROS node's ingest (bonxai_server.cpp:147-168): drops
+ * non-finite points and applies a row-major 3x4 float transform. Port
+ * library only (the node and PCL are not part of the compiled reference). */
+size_t orc_sensor_to_world_f32(const float* m12, const float* xyz, size_t n, float* out);
 
 /* ---------------- VoxelGrid<T> ---------------- */
 void* orc_grid_create(double voxel_size, int inner_bits, int leaf_bits, int dtype);

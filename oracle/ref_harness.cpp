@@ -43,6 +43,7 @@
 
 #define private public
 #include "bonxai/bonxai.hpp"
+#include "bonxai/serialization.hpp"
 #include "bonxai_map/probabilistic_map.hpp"
 #undef private
 
@@ -121,6 +122,7 @@ struct GridBase {
   virtual size_t dump(int32_t* xyz, void* v, size_t cap) = 0;
   virtual void clear(int opt) = 0;
   virtual void release() = 0;
+  virtual std::string serialize() = 0;
 };
 
 template <typename T>
@@ -202,6 +204,11 @@ struct RefGrid : GridBase {
   void release() override {
     grid.releaseUnusedMemory();
     accp.reset(new Acc(grid.createAccessor()));
+  }
+  std::string serialize() override {
+    std::ostringstream os(std::ios::binary);
+    Bonxai::Serialize(os, grid);
+    return os.str();
   }
 };
 
@@ -334,6 +341,24 @@ size_t orc_pmap_get_occupied(void* m, int32_t* xyz, size_t cap) {
   return copy_coords(v, xyz, cap);
 }
 
+size_t orc_pmap_export_occupied_f32(void* m, double min_z, double max_z, float* xyz,
+                                    size_t cap) {
+  // the reference's PointT overload (coordToPos), then the node's z band
+  std::vector<ProbabilisticMap::Vector3D> v;
+  static_cast<RefPMap*>(m)->map.getOccupiedVoxels(v);
+  size_t k = 0;
+  for (const auto& p : v) {
+    if (!(p.z() >= min_z && p.z() <= max_z)) continue;
+    if (k < cap) {
+      xyz[3 * k] = float(p.x());
+      xyz[3 * k + 1] = float(p.y());
+      xyz[3 * k + 2] = float(p.z());
+    }
+    k++;
+  }
+  return k;
+}
+
 size_t orc_pmap_get_free(void* m, int32_t* xyz, size_t cap) {
   std::vector<CoordT> v;
   static_cast<RefPMap*>(m)->map.getFreeVoxels(v);
@@ -378,6 +403,21 @@ size_t orc_grid_dump(void* g, int32_t* xyz, void* v, size_t cap) {
 }
 void orc_grid_clear(void* g, int opt) { static_cast<GridBase*>(g)->clear(opt); }
 void orc_grid_release_unused(void* g) { static_cast<GridBase*>(g)->release(); }
+
+/* Reference-only: Bonxai::Serialize of a grid or of a map's grid
+ * (serialization.hpp:77-116). Returns the byte count; writes up to cap. */
+size_t orc_ref_grid_serialize(void* g, char* out, size_t cap) {
+  const std::string s = static_cast<GridBase*>(g)->serialize();
+  if (out) std::memcpy(out, s.data(), std::min(cap, s.size()));
+  return s.size();
+}
+size_t orc_ref_pmap_serialize(void* m, char* out, size_t cap) {
+  std::ostringstream os(std::ios::binary);
+  Bonxai::Serialize(os, static_cast<RefPMap*>(m)->map.grid());
+  const std::string s = os.str();
+  if (out) std::memcpy(out, s.data(), std::min(cap, s.size()));
+  return s.size();
+}
 
 size_t orc_compute_ray(const int32_t* o, const int32_t* e, int32_t* out, size_t cap) {
   std::vector<CoordT> ray;

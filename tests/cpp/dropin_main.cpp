@@ -14,7 +14,13 @@
 #include <string>
 #include <vector>
 
+#include <algorithm>
+#include <cmath>
+#include <sstream>
+#include <tuple>
+
 #include "bonxai/bonxai.hpp"
+#include "bonxai/serialization.hpp"
 #include "bonxai_map/probabilistic_map.hpp"
 
 struct PointXYZ {  // pcl::PointXYZ layout: x, y, z and padding
@@ -78,6 +84,28 @@ static int tutorial(const std::string& out) {
   f << "const_below " << (cell ? std::to_string(*cell) : std::string("nullptr")) << "\n";
   f << "binary_on " << binaryGrid.createConstAccessor().isCellOn(grid.posToCoord(0.55, 0.55, 0.55))
     << "\n";
+
+  // serialization round trip (the reference's examples/test_serialization.cpp
+  // flow): Serialize, read the header line, GetHeaderInfo, Deserialize
+  std::ostringstream ofile(std::ios::binary);
+  Bonxai::Serialize(ofile, grid);
+  Bonxai::Serialize(ofile, grid);  // two grids in one stream
+  std::istringstream ifile(ofile.str(), std::ios::binary);
+  char header[256];
+  ifile.getline(header, 256);
+  Bonxai::HeaderInfo info = Bonxai::GetHeaderInfo(header);
+  auto new_grid = Bonxai::Deserialize<long>(ifile, info);
+  ifile.getline(header, 256);
+  auto third = Bonxai::Deserialize<long>(ifile, Bonxai::GetHeaderInfo(header));
+  bool same = new_grid.activeCellsCount() == grid.activeCellsCount() &&
+              third.activeCellsCount() == grid.activeCellsCount();
+  auto na = new_grid.createConstAccessor();
+  grid.forEachCell([&](const long& v, const Bonxai::CoordT& c) {
+    const long* p = na.value(c);
+    if (!p || *p != v) same = false;
+  });
+  f << "serialization " << info.type_name << " " << info.inner_bits << " " << info.leaf_bits
+    << " " << (same ? "round_trip_ok" : "round_trip_bad") << "\n";
   return 0;
 }
 
@@ -90,15 +118,55 @@ static int lidar(const std::string& in, const std::string& outdir) {
   f.read(reinterpret_cast<char*>(&res), 8);
   f.read(reinterpret_cast<char*>(&max_range), 8);
   Bonxai::ProbabilisticMap map(res);
+  // the ROS node's flow: sensor-frame clouds + pose (identity rotation here),
+  // against insertPointCloud of the same world points
+  Bonxai::ProbabilisticMap node_map(res), plain_map(res);
+  struct Pose {
+    float m[3][4];
+    float operator()(int r, int c) const { return m[r][c]; }
+  };
   std::vector<float> buf(size_t(n_points) * 3);
   for (int s = 0; s < n_scans; s++) {
     float o[3];
     f.read(reinterpret_cast<char*>(o), 12);
     f.read(reinterpret_cast<char*>(buf.data()), buf.size() * 4);
-    std::vector<PointXYZ> cloud;
+    std::vector<PointXYZ> cloud, sensor, world;
     cloud.reserve(n_points);
-    for (int i = 0; i < n_points; i++) cloud.emplace_back(buf[3 * i], buf[3 * i + 1], buf[3 * i + 2]);
+    for (int i = 0; i < n_points; i++) {
+      cloud.emplace_back(buf[3 * i], buf[3 * i + 1], buf[3 * i + 2]);
+      sensor.emplace_back(buf[3 * i] - o[0], buf[3 * i + 1] - o[1], buf[3 * i + 2] - o[2]);
+      world.emplace_back(sensor.back().x + o[0], sensor.back().y + o[1], sensor.back().z + o[2]);
+    }
+    sensor.emplace_back(std::nanf(""), 0.f, 0.f);  // dropped by the ingest
     map.insertPointCloud(cloud, PointXYZ(o[0], o[1], o[2]), max_range);
+    const Pose pose{{{1, 0, 0, o[0]}, {0, 1, 0, o[1]}, {0, 0, 1, o[2]}}};
+    node_map.insertSensorCloud(sensor, pose, max_range);
+    plain_map.insertPointCloud(world, PointXYZ(o[0], o[1], o[2]), max_range);
+  }
+  {
+    std::vector<Bonxai::CoordT> a, b;
+    node_map.getOccupiedVoxels(a);
+    plain_map.getOccupiedVoxels(b);
+    auto key = [](const Bonxai::CoordT& c) { return std::make_tuple(c.x, c.y, c.z); };
+    auto less = [&](const Bonxai::CoordT& l, const Bonxai::CoordT& r) { return key(l) < key(r); };
+    std::sort(a.begin(), a.end(), less);
+    std::sort(b.begin(), b.end(), less);
+    bool same = a.size() == b.size() && node_map.grid().activeCellsCount() ==
+                                            plain_map.grid().activeCellsCount();
+    for (size_t i = 0; same && i < a.size(); i++) same = key(a[i]) == key(b[i]);
+    // the export: float corner positions of the occupied cells
+    std::vector<float> pos(node_map.countOccupied(-1e30, 1e30) * 3);
+    const size_t n_exp = node_map.exportOccupied(pos.data(), pos.size() / 3, -1e30, 1e30);
+    std::vector<Bonxai::Point3D> want;
+    node_map.getOccupiedVoxels(want);
+    std::vector<std::tuple<float, float, float>> pe, pw;
+    for (size_t i = 0; i < n_exp; i++) pe.emplace_back(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]);
+    for (const auto& p : want) pw.emplace_back(float(p.x), float(p.y), float(p.z));
+    std::sort(pe.begin(), pe.end());
+    std::sort(pw.begin(), pw.end());
+    std::ofstream fn(outdir + "/node.txt");
+    fn << "ingest " << (same ? "same" : "differs") << " export "
+       << (pe == pw && n_exp > 0 ? "same" : "differs") << "\n";
   }
   // hit and miss points by hand, then the free-space rays
   for (int i = 0; i < 200; i++) {

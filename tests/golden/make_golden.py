@@ -18,6 +18,8 @@ Fixtures
   pmap_addpts.npz   addHitPoint/addMissPoint batches then updateFreeCells.
   grid_setvalue.npz VoxelGrid<float> and <int32> setValue with duplicates
                     (last writer wins), value(create), setCellOn/Off, was_on.
+  serialized.npz    the reference's Serialize byte streams of a VoxelGrid<float>
+                    and of a ProbabilisticMap's grid after 3 LiDAR scans.
   constants.npz     default Options (logods of 0.4, 0.7, 0.12, 0.97, 0.5).
 """
 from __future__ import annotations
@@ -139,6 +141,21 @@ def main():
                     f"{name}_active": g.active_cells()})
     out["points"] = pts
     np.savez_compressed(HERE / "grid_setvalue.npz", **out)
+
+    # ---- Serialize (serialization.hpp:77-116) of a grid and of a map's grid
+    gpts = np.load(HERE / "grid_setvalue.npz")["points"]
+    g = R.grid(0.05, 2, 3, O.ORC_F32)
+    gc = g.pos_to_coord(gpts)
+    gv = (np.random.default_rng(3).random(len(gpts)) * 1000).astype(np.float32)
+    g.set_values(gc, gv)
+    m = R.pmap(scene.resolution)
+    lid = np.load(HERE / "pmap_lidar.npz")
+    for k in range(3):
+        m.insert(lid["points"][k], lid["origins"][k], float(lid["max_range"]))
+    np.savez_compressed(HERE / "serialized.npz",
+                        grid_f32=np.frombuffer(g.serialize_reference(), np.uint8),
+                        grid_coords=gc, grid_values=gv,
+                        pmap=np.frombuffer(m.serialize_reference(), np.uint8))
 
     # ---- constants
     m = R.pmap(0.1)

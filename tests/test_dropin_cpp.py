@@ -70,6 +70,8 @@ def test_dropin_program_matches_oracle(dropin_exe, tmp_path, port):
     assert lines["const_origin"] == "1"
     assert lines["const_below"] == "nullptr"
     assert lines["binary_on"] == "1"
+    assert lines["serialization"] == "long 2 3 round_trip_ok"
+    assert (tmp_path / "node.txt").read_text().split() == ["ingest", "same", "export", "same"]
 
     # --- probabilistic map flow
     m = port.pmap(scene.resolution)

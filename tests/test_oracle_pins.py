@@ -171,3 +171,62 @@ def test_pos_to_coord_edges(port, ref):
                     [123.456, -987.65, 0.05]], np.float64)
     for res in (0.02, 0.05, 0.1, 0.3):
         assert np.array_equal(port.grid(res).pos_to_coord(pts), ref.grid(res).pos_to_coord(pts))
+
+
+def test_serialized_streams_golden(port):
+    """The reference's Serialize streams hold exactly the cells the restatement
+    builds from the same inputs (format read by tests/serial_format.py)."""
+    import serial_format as sf
+    g = golden("serialized.npz")
+    header, xyz, vals = sf.parse(g["grid_f32"].tobytes(), 4)
+    assert header == "Bonxai::VoxelGrid<float,2,3>(0.050000)"
+    G = port.grid(0.05, 2, 3, 0)
+    G.set_values(g["grid_coords"], g["grid_values"])
+    ox, ov = G.dump()
+    assert np.array_equal(xyz, ox) and np.array_equal(vals.view(np.float32).ravel(), ov)
+    header, xyz, vals = sf.parse(g["pmap"].tobytes(), 4)
+    assert header == "Bonxai::VoxelGrid<Bonxai::ProbabilisticMap::CellT,2,3>(0.100000)"
+    lid = golden("pmap_lidar.npz")
+    m = port.pmap(0.1)
+    for k in range(3):
+        m.insert(lid["points"][k], lid["origins"][k], float(lid["max_range"]))
+    ox, oc = m.dump()
+    assert np.array_equal(xyz, ox) and np.array_equal(vals.view(np.int32).ravel(), oc)
+
+
+@pytest.mark.parametrize("zband", [(-np.inf, np.inf), (0.0, 2.0), (0.35, 0.35)])
+def test_port_export_occupied_matches_reference(port, ref, zband):
+    """The restated occupied-point export equals the reference's PointT
+    getOccupiedVoxels (coordToPos) with the ROS node's z band applied."""
+    scene = synth.LidarScene()
+    a, b = port.pmap(0.1), ref.pmap(0.1)
+    for k in range(3):
+        pts, o = scene.scan(k, n_points=20000)
+        a.insert(pts, o, 30.0)
+        b.insert(pts, o, 30.0)
+    ea, eb = a.export_occupied(*zband), b.export_occupied(*zband)
+    assert len(ea) > 0 or zband == (0.35, 0.35)
+    assert np.array_equal(ea.view(np.uint32), eb.view(np.uint32))
+
+
+def test_sensor_to_world_restatement(port):
+    """Non-finite points are dropped in order; the transform is float with the
+    stated order ((r0*x + r1*y) + r2*z) + t, checked against numpy float32."""
+    rng = np.random.default_rng(3)
+    p = rng.normal(0, 10, (5000, 3)).astype(np.float32)
+    p[7, 1] = np.nan
+    p[11, 2] = np.inf
+    p[12, 0] = -np.inf
+    c, s = np.cos(0.3), np.sin(0.3)
+    m = np.array([[c, -s, 0.0, 1.25], [s, c, 0.0, -3.5], [0.0, 0.0, 1.0, 1.7]], np.float32)
+    got = port.sensor_to_world(m, p)
+    keep = np.isfinite(p).all(axis=1)
+    q = p[keep]
+    want = np.empty_like(q)
+    for r in range(3):
+        v = m[r, 0] * q[:, 0]
+        v = v + m[r, 1] * q[:, 1]
+        v = v + m[r, 2] * q[:, 2]
+        want[:, r] = v + m[r, 3]
+    assert got.dtype == np.float32 and len(got) == keep.sum()
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))

@@ -58,22 +58,39 @@ def test_same_alone_and_in_the_mix(gpu, port):
     srv = gpu.Server(res)
     stop = threading.Event()
 
+    noise_ids = (0, 1, 2, 4, 5)
+    started = threading.Barrier(len(noise_ids) + 1)
+
     def noise(cid):
+        # the load is generated up front, so that it is in flight while
+        # client 0's requests run
         rng = np.random.default_rng(cid)
         sc = synth.LidarScene(seed=9200 + cid)
-        k = 0
-        while not stop.is_set():
+        work = []
+        for k in range(6):
             if rng.random() < 0.6:
-                pts, o = sc.scan(k % 20, n_points=int(rng.integers(2000, 20000)))
-                srv.insert(cid, pts, o, 30.0, discard=True)
-                k += 1
+                work.append(("i",) + sc.scan(k, n_points=int(rng.integers(2000, 8000))))
             else:
-                q = rng.integers(-100, 100, (int(rng.integers(100, 50000)), 3)).astype(np.int32)
-                srv.query(cid, q, mode=int(rng.integers(0, 3)), discard=True)
+                n = int(rng.integers(100, 50000))
+                work.append(("q", rng.integers(-100, 100, (n, 3)).astype(np.int32),
+                             int(rng.integers(0, 3))))
+        first = True
+        k = 0
+        while (first or not stop.is_set()) and k < 200:
+            w = work[k % len(work)]
+            if w[0] == "i":
+                srv.insert(cid, w[1], w[2], 30.0, discard=True)
+            else:
+                srv.query(cid, w[1], mode=w[2], discard=True)
+            k += 1
+            if first:
+                started.wait(timeout=120)
+                first = False
 
-    threads = [threading.Thread(target=noise, args=(c,)) for c in (0, 1, 2, 4, 5)]
+    threads = [threading.Thread(target=noise, args=(c,)) for c in noise_ids]
     for th in threads:
         th.start()
+    started.wait(timeout=120)
     tickets = [_submit(srv, 3, r) for r in seq]
     mixed = [_collect(srv, r, t) for r, t in zip(seq, tickets)]
     stop.set()
