@@ -32,8 +32,6 @@ SET_ALL_CELLS_OFF = 1
 FLAG_KEEP_NONFINITE = 1
 FLAG_TIMING = 2
 FLAG_NO_GRAPH = 4
-FLAG_RAY_CHUNKS = 8
-FLAG_LEAF_CACHE = 16
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "node pool exhausted", 3: "root hash full",
           4: "device wait timed out", 5: "CUDA error", 6: "no CUDA device",

@@ -33,6 +33,7 @@ constexpr uint32_t kMaxTickScans = 128;
 // Layout of the per-tick meta buffer; bytes [0, kBackBytes) are read back.
 constexpr size_t kOffBar = 0;                                    // 2 x u32
 constexpr size_t kOffErr = 8;                                    // u32
+constexpr size_t kOffRayNext = 12;                               // u32
 constexpr size_t kOffTime = 16;                                  // [8] u64 phase timestamps
 constexpr size_t kOffStats = 80;                                 // [128][4] u64
 constexpr size_t kOffCnt = kOffStats + kMaxTickScans * 32;       // [128] u32
@@ -64,6 +65,7 @@ struct TickArgs {
   uint32_t* ray_prefix;       // [n_scans + 1]
   uint32_t* bar;              // barrier: arrivals, generation
   uint32_t* err;              // barrier timeout
+  uint32_t* ray_next;         // next ray a group takes in phase 4 (zeroed per tick)
   uint32_t* ctr_out;          // [n_scans][C_WORDS]
   unsigned long long* times;  // [8] global-timer stamps at each phase boundary
   uint32_t n_scans;
@@ -241,11 +243,16 @@ __global__ void __launch_bounds__(256, U == 2 ? 3 : 4) k_tick(const TickArgs* __
     const unsigned sl = lane & (W - 1);
     const unsigned gbase = lane & ~(W - 1);
     const unsigned gmask = (W == 32) ? 0xffffffffu : (((1u << W) - 1u) << gbase);
-    const uint32_t gid = static_cast<uint32_t>(gtid / W);
-    const uint32_t ngroups = static_cast<uint32_t>(gsize / W);
     const uint32_t total = ld_volatile(A.ray_prefix + ns);
     uint32_t visited = 0, updated = 0, cur = kNone;
-    for (uint32_t r = gid; r < total; r += ngroups) {
+    // rays are taken dynamically (lengths vary widely); the leader takes the
+    // next one before walking the current one
+    uint32_t r = 0;
+    if (sl == 0) r = atomicAdd(A.ray_next, 1u);
+    r = __shfl_sync(gmask, r, 0, W);
+    while (r < total) {
+      uint32_t nr = 0;
+      if (sl == 0) nr = atomicAdd(A.ray_next, 1u);
       const uint32_t s = scan_of_ray(A.ray_prefix, ns, r);
       if (s != cur) {
         if (cur != kNone) {
@@ -266,6 +273,7 @@ __global__ void __launch_bounds__(256, U == 2 ? 3 : 4) k_tick(const TickArgs* __
       else
         walk_ray<W>(S.M, e, S.ox, S.oy, S.oz, S.u, S.o.miss, S.o.cmin, sl, gbase, gmask,
                     visited, updated);
+      r = __shfl_sync(gmask, nr, 0, W);
     }
     if (cur != kNone) {
       const uint32_t v = __reduce_add_sync(gmask, visited), up = __reduce_add_sync(gmask, updated);
@@ -388,7 +396,7 @@ cudaError_t enqueue_tick(bxg_batch b, size_t param_bytes, size_t smem) {
   cudaError_t e = cudaMemcpyAsync(b->params.p, b->h_args, param_bytes, cudaMemcpyHostToDevice,
                                   b->stream);
   if (e != cudaSuccess) return e;
-  e = cudaMemsetAsync(b->meta.p, 0, 16, b->stream);  // barrier words and error word
+  e = cudaMemsetAsync(b->meta.p, 0, 16, b->stream);  // barrier, error and ray-counter words
   if (e != cudaSuccess) return e;
   e = launch_for(b, smem);
   if (e != cudaSuccess) return e;
@@ -514,6 +522,7 @@ int bxg_batch_insert_f32(bxg_batch b, const bxg_pmap* maps, size_t n_scans, cons
   A.cast = b->cast.as<int4>();
   A.bar = reinterpret_cast<uint32_t*>(meta + kOffBar);
   A.err = reinterpret_cast<uint32_t*>(meta + kOffErr);
+  A.ray_next = reinterpret_cast<uint32_t*>(meta + kOffRayNext);
   A.stats = reinterpret_cast<unsigned long long*>(meta + kOffStats);
   A.cast_cnt = reinterpret_cast<uint32_t*>(meta + kOffCnt);
   A.ctr_out = reinterpret_cast<uint32_t*>(meta + kOffCtr);

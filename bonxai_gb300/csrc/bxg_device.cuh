@@ -67,7 +67,9 @@ enum : int {
 enum : int { S_POINTS = 0, S_RAY_LEN = 1, S_VISITED = 2, S_UPDATED = 3, S_COUNT = 12 };
 
 // Kinds of endpoint.
-enum : int32_t { EP_HIT = 0, EP_MISS = 1, EP_SKIP = 2 };
+// EP_DUP: a valid point whose endpoint cell a lower index in its warp also
+// reaches (it counts as a point but cannot decide the cell).
+enum : int32_t { EP_HIT = 0, EP_MISS = 1, EP_SKIP = 2, EP_DUP = 3 };
 
 struct DMap {
   // geometry (bonxai.hpp:117-123)

@@ -33,11 +33,22 @@ __global__ void k_endpoints(DMap M, const uint8_t* __restrict__ pts, size_t stri
                             double inv_res, int keep_nonfinite, int4* __restrict__ ep,
                             uint4* tab, uint32_t tmask) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const PT* p = reinterpret_cast<const PT*>(pts + size_t(i) * stride);
-  const int4 e = compute_endpoint<PT>(p, fx, fy, fz, max_range, mr2, inv_res, keep_nonfinite != 0);
-  ep[i] = e;
-  if (e.w != EP_SKIP) dedup_min_insert(tab, tmask, e.x, e.y, e.z, i, M);
+  int4 e = make_int4(0, 0, 0, EP_SKIP);
+  if (i < n) {
+    const PT* p = reinterpret_cast<const PT*>(pts + size_t(i) * stride);
+    e = compute_endpoint<PT>(p, fx, fy, fz, max_range, mr2, inv_res, keep_nonfinite != 0);
+  }
+  // Neighbouring points often share an endpoint cell: within a warp only the
+  // lowest lane (lowest index) of each cell enters the table; the others can
+  // never be the cell's lowest index and are marked EP_DUP.
+  const unsigned vm = __ballot_sync(0xffffffffu, e.w != EP_SKIP);
+  if (e.w != EP_SKIP) {
+    const unsigned same = __match_any_sync(vm, e.x) & __match_any_sync(vm, e.y) &
+                          __match_any_sync(vm, e.z);
+    if (same & ((1u << (threadIdx.x & 31)) - 1u)) e.w = EP_DUP;
+    else dedup_min_insert(tab, tmask, e.x, e.y, e.z, i, M);
+  }
+  if (i < n) ep[i] = e;
 }
 
 // A sensor-frame cloud with its sensor-to-world transform (row-major 3x4),
@@ -100,7 +111,9 @@ __global__ void k_winners(DMap M, const int4* __restrict__ ep, uint32_t n,
   int4 e = make_int4(0, 0, 0, EP_SKIP);
   if (i < n) {
     e = ep[i];
-    if (e.w != EP_SKIP && dedup_lookup(tab, tmask, e.x, e.y, e.z) == i) add = winner_apply(M, e, u, o);
+    if (e.w == EP_HIT || e.w == EP_MISS) {
+      if (dedup_lookup(tab, tmask, e.x, e.y, e.z) == i) add = winner_apply(M, e, u, o);
+    }
   }
   const unsigned lane = threadIdx.x & 31;
   const unsigned valid = __ballot_sync(0xffffffffu, i < n && e.w != EP_SKIP);
@@ -149,14 +162,10 @@ __global__ void k_apply(DMap M, const int4* __restrict__ cast, uint32_t cast_cap
 
 // Ray phase: one group of W lanes per listed ray (walk_ray, or walk_ray2 with
 // two cells per lane per step when U == 2).
-// CHUNK: each group takes a contiguous run of the ray list instead of every
-// ngroups-th ray (neighbouring rays share leaves). CACHE (W = 32, U = 1): a
-// per-warp leaf cache in shared memory (walk_ray_op).
-template <int W, int U, bool CHUNK = false, bool CACHE = false>
+template <int W, int U>
 __global__ void __launch_bounds__(256, U == 2 ? 3 : 4) k_rays(DMap M, const int4* __restrict__ cast,
                                                  uint32_t cast_cap, int ox, int oy, int oz,
                                                  int32_t u, int32_t miss, int32_t cmin) {
-  extern __shared__ uint4 k_rays_smem[];
   const uint32_t n_cast = min(ld_volatile(M.ctr + C_CAST), cast_cap);
   const unsigned lane = threadIdx.x & 31;
   const unsigned sl = lane & (W - 1);
@@ -164,25 +173,12 @@ __global__ void __launch_bounds__(256, U == 2 ? 3 : 4) k_rays(DMap M, const int4
   const unsigned gmask = (W == 32) ? 0xffffffffu : (((1u << W) - 1u) << gbase);
   const uint32_t gid = (blockIdx.x * blockDim.x + threadIdx.x) / W;
   const uint32_t ngroups = (gridDim.x * blockDim.x) / W;
-  uint4* lc = nullptr;
-  if (CACHE) {
-    lc = k_rays_smem + (threadIdx.x / 32) * kLeafCache;
-    for (int i = lane; i < kLeafCache; i += 32) lc[i] = make_uint4(kNone, kNone, kNone, kNone);
-    __syncwarp();
-  }
-  uint32_t r = gid, r_end = n_cast, r_step = ngroups;
-  if (CHUNK) {
-    const uint32_t chunk = (n_cast + ngroups - 1) / ngroups;
-    r = min(gid * chunk, n_cast);
-    r_end = min(r + chunk, n_cast);
-    r_step = 1;
-  }
   uint32_t visited = 0, updated = 0;
-  for (; r < r_end; r += r_step) {
+  for (uint32_t r = gid; r < n_cast; r += ngroups) {
     if (U == 2)
       walk_ray2<W>(M, cast[r], ox, oy, oz, u, miss, cmin, sl, gbase, gmask, visited, updated);
     else
-      walk_ray<W>(M, cast[r], ox, oy, oz, u, miss, cmin, sl, gbase, gmask, visited, updated, lc);
+      walk_ray<W>(M, cast[r], ox, oy, oz, u, miss, cmin, sl, gbase, gmask, visited, updated);
   }
   visited = __reduce_add_sync(0xffffffffu, visited);
   updated = __reduce_add_sync(0xffffffffu, updated);
@@ -333,18 +329,6 @@ int launch_rays(bxg_pmap_s* pm, int ox, int oy, int oz) {
   const dim3 g{unsigned(blocks)}, b{unsigned(bs)};
   const int4* c = m->s_cast.as<int4>();
   const int32_t uc = pm->update_count;
-  const bool chunk = m->flags & BXG_FLAG_RAY_CHUNKS, cache = m->flags & BXG_FLAG_LEAF_CACHE;
-  if (rpw == 1 && !u2 && (chunk || cache)) {
-    const size_t smem = cache ? size_t(bs / 32) * kLeafCache * sizeof(uint4) : 0;
-    if (chunk && cache)
-      k_rays<32, 1, true, true><<<g, b, smem, m->stream>>>(m->dm, c, ccap, ox, oy, oz, uc, o.miss, o.cmin);
-    else if (chunk)
-      k_rays<32, 1, true, false><<<g, b, 0, m->stream>>>(m->dm, c, ccap, ox, oy, oz, uc, o.miss, o.cmin);
-    else
-      k_rays<32, 1, false, true><<<g, b, smem, m->stream>>>(m->dm, c, ccap, ox, oy, oz, uc, o.miss, o.cmin);
-    BXG_LAUNCHED(m);
-    return BXG_OK;
-  }
   if (rpw == 4) {
     if (u2) k_rays<8, 2><<<g, b, 0, m->stream>>>(m->dm, c, ccap, ox, oy, oz, uc, o.miss, o.cmin);
     else k_rays<8, 1><<<g, b, 0, m->stream>>>(m->dm, c, ccap, ox, oy, oz, uc, o.miss, o.cmin);

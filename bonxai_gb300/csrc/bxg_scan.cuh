@@ -142,26 +142,10 @@ __device__ __forceinline__ bool winner_apply(const DMap& M, int4 e, int32_t u, c
 // op(act, leaf, ci, k): act = the lane has a cell (k < m), leaf = its leaf
 // slot (kNone if the pool ran out), ci = its index in the leaf, k = its
 // position on the ray.
-//
-// With a leaf cache (lcache != nullptr, W == 32 only) a warp keeps the leaf
-// slots it resolved in a direct-mapped table of kLeafCache entries in shared
-// memory, {leaf key xyz, slot}; a head looks there before the root hash.
-// Slots never move while a kernel runs (pools grow only between launches), so
-// an entry stays valid for the whole launch. One lane per entry writes in a
-// step (the lowest lane of those that map to it), so no entry is torn.
-constexpr int kLeafCache = 64;
-
-__device__ __forceinline__ uint32_t leaf_cache_slot(int lx, int ly, int lz, int lb) {
-  const uint32_t h = static_cast<uint32_t>(lx >> lb) * 0x9E3779B1u ^
-                     static_cast<uint32_t>(ly >> lb) * 0x85EBCA77u ^
-                     static_cast<uint32_t>(lz >> lb) * 0xC2B2AE3Du;
-  return (h ^ (h >> 16)) & (kLeafCache - 1);
-}
-
 template <int W, class Op>
 __device__ __forceinline__ void walk_ray_op(const DMap& M, int4 e, int ox, int oy, int oz,
                                             unsigned sl, unsigned gbase, unsigned gmask,
-                                            Op&& op, uint4* lcache = nullptr) {
+                                            Op&& op) {
   const int dx = e.x - ox, dy = e.y - oy, dz = e.z - oz;
   const uint32_t ax = static_cast<uint32_t>(abs(dx)), ay = static_cast<uint32_t>(abs(dy)),
                  az = static_cast<uint32_t>(abs(dz));
@@ -198,46 +182,23 @@ __device__ __forceinline__ void walk_ray_op(const DMap& M, int4 e, int ox, int o
     const bool head = act && key != q;
     uint32_t leaf = kNone, in = kNone;
     bool root_miss = false;
-    bool cache_put = false;
-    uint32_t cslot = 0;
-    const int32_t lmk = leaf_mask(M);
     if (head) {
-      bool hit = false;
-      if (W == 32 && lcache) {
-        cslot = leaf_cache_slot(cx & lmk, cy & lmk, cz & lmk, lb);
-        const uint4 ce = lcache[cslot];
-        if (static_cast<int>(ce.x) == (cx & lmk) && static_cast<int>(ce.y) == (cy & lmk) &&
-            static_cast<int>(ce.z) == (cz & lmk)) {
-          leaf = ce.w;
-          hit = true;
+      const int rx = cx & rm, ry = cy & rm, rz = cz & rm;
+      if (rx == rkx && ry == rky && rz == rkz) {
+        in = rin;
+      } else {
+        root_miss = true;
+        in = root_probe_fast(M, rx, ry, rz);
+        if (in == kPending) in = root_get_or_create(M, rx, ry, rz);
+      }
+      if (in != kNone) {
+        const uint32_t ii = inner_index(M, cx, cy, cz);
+        leaf = M.ichild[static_cast<size_t>(in) * M.isize + ii];
+        if (leaf >= kPending) {
+          const int32_t lm = leaf_mask(M);
+          leaf = leaf_get_or_create(M, in, ii, cx & lm, cy & lm, cz & lm);
         }
       }
-      if (!hit) {
-        const int rx = cx & rm, ry = cy & rm, rz = cz & rm;
-        if (rx == rkx && ry == rky && rz == rkz) {
-          in = rin;
-        } else {
-          root_miss = true;
-          in = root_probe_fast(M, rx, ry, rz);
-          if (in == kPending) in = root_get_or_create(M, rx, ry, rz);
-        }
-        if (in != kNone) {
-          const uint32_t ii = inner_index(M, cx, cy, cz);
-          leaf = M.ichild[static_cast<size_t>(in) * M.isize + ii];
-          if (leaf >= kPending) leaf = leaf_get_or_create(M, in, ii, cx & lmk, cy & lmk, cz & lmk);
-        }
-        cache_put = leaf != kNone;
-      }
-    }
-    if (W == 32 && lcache) {
-      const unsigned pm = __ballot_sync(0xffffffffu, cache_put);
-      if (cache_put) {
-        const unsigned peers = __match_any_sync(pm, cslot);
-        if ((peers & ((1u << sl) - 1u)) == 0)
-          lcache[cslot] = make_uint4(static_cast<uint32_t>(cx & lmk), static_cast<uint32_t>(cy & lmk),
-                                     static_cast<uint32_t>(cz & lmk), leaf);
-      }
-      __syncwarp();
     }
     const unsigned hm = (__ballot_sync(gmask, head) & gmask) >> gbase;
     const unsigned below = hm & ((2u << sl) - 1u);
@@ -267,7 +228,7 @@ template <int W>
 __device__ __forceinline__ void walk_ray(const DMap& M, int4 e, int ox, int oy, int oz,
                                          int32_t u, int32_t miss, int32_t cmin, unsigned sl,
                                          unsigned gbase, unsigned gmask, uint32_t& visited,
-                                         uint32_t& updated, uint4* lcache = nullptr) {
+                                         uint32_t& updated) {
   int32_t* const cells = reinterpret_cast<int32_t*>(M.ldata);
   walk_ray_op<W>(M, e, ox, oy, oz, sl, gbase, gmask,
                  [&](bool act, uint32_t leaf, uint32_t ci, uint32_t) {
@@ -281,8 +242,7 @@ __device__ __forceinline__ void walk_ray(const DMap& M, int4 e, int ox, int oy, 
                      }
                      visited++;
                    }
-                 },
-                 lcache);
+                 });
 }
 
 // Leaf slot of a head cell: the group's cached root when it matches, else the

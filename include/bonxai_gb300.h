@@ -73,11 +73,6 @@ typedef struct {
 #define BXG_FLAG_TIMING 2u
 /* Batched ticks: launch directly instead of replaying a captured CUDA graph. */
 #define BXG_FLAG_NO_GRAPH 4u
-/* Per-map ray kernel shape (rays_per_warp 1, ray_unroll 1): each warp walks a
- * contiguous run of the ray list; and/or keeps a leaf-slot cache in shared
- * memory. Same results. */
-#define BXG_FLAG_RAY_CHUNKS 8u
-#define BXG_FLAG_LEAF_CACHE 16u
 
 void bxg_config_default(bxg_config* cfg);
 const char* bxg_status_string(int status);

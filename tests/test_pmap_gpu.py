@@ -70,35 +70,6 @@ def test_lidar_scans_vs_oracle(gpu, port, rpw, unroll):
     assert_same_map(m, o)
 
 
-@pytest.mark.parametrize("flags", [8, 16, 24])
-def test_ray_chunks_and_leaf_cache_vs_oracle(gpu, port, flags):
-    """Contiguous ray runs per warp and the per-warp leaf cache change no
-    result: LiDAR sequence, depth frames at 0.02 m and the golden fixture."""
-    scene = synth.LidarScene()
-    m = gpu.ProbabilisticMap(scene.resolution, gpu.Config(flags=flags | gpu.FLAG_TIMING))
-    o = port.pmap(scene.resolution)
-    for k in range(5):
-        pts, org = scene.scan(k, n_points=16384)
-        v = m.insert_point_cloud(pts, org, scene.max_range)
-        assert v == o.insert(pts, org, scene.max_range)
-        assert m.last_stats()["ray_cells_visited"] == v - 16384
-    assert_same_map(m, o)
-    room = synth.DepthRoom()
-    m2 = gpu.ProbabilisticMap(room.resolution, gpu.Config(flags=flags))
-    o2 = port.pmap(room.resolution)
-    for k in range(3):
-        pts, org = room.frame(k, subsample=8)
-        assert m2.insert_point_cloud(pts, org, room.max_range) == o2.insert(pts, org, room.max_range)
-    assert_same_map(m2, o2)
-    g = golden("pmap_lidar.npz")
-    m3 = gpu.ProbabilisticMap(float(g["resolution"]), gpu.Config(flags=flags))
-    for k in range(len(g["points"])):
-        assert m3.insert_point_cloud(g["points"][k], g["origins"][k],
-                                     float(g["max_range"])) == g["v"][k]
-    xyz, c = m3.dump()
-    assert np.array_equal(xyz, g["xyz8"]) and np.array_equal(c, g["cells8"])
-
-
 def test_depth_frames_vs_oracle(gpu, port):
     room = synth.DepthRoom()
     m = gpu.ProbabilisticMap(room.resolution)
