@@ -288,6 +288,7 @@ int build_dedup(MapCore* m, const int32_t* dxyz, uint32_t n, bool keep_max, bool
   const uint32_t cap = next_pow2(uint64_t(n) * 2);
   BXG_CUDA(m, m->s_dedup.ensure(size_t(cap) * 16));
   launch_dedup_clear(m, m->s_dedup.as<uint4>(), cap);
+  m->dedup_clean = 0;  // a ProbabilisticMap scan on this core must clear it again
   uint32_t* tmin = nullptr;
   if (need_min) {
     BXG_CUDA(m, m->s_dedup2.ensure(size_t(cap) * 4 + size_t(cap)));

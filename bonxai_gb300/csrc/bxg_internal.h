@@ -81,6 +81,10 @@ struct MapCore {
 
   // scratch
   DevBuf s_in, s_in2, s_out, s_out2, s_dedup, s_dedup2, s_ep, s_cast, s_tmp;
+  // entries of s_dedup known to be empty, from index 0 (the ray kernel clears
+  // the table the last endpoint phase used, so the next one needs no memset)
+  uint32_t dedup_clean = 0;
+  uint32_t dedup_used = 0;  // entries the last endpoint phase used
 
   std::string err;
   uint64_t launches = 0;

@@ -27,11 +27,18 @@
 namespace bxg {
 
 // Endpoint of each point; lowest index per endpoint cell in the scratch table.
+// zero_stats: the scan's statistics start at zero (saves a memset).
+__device__ __forceinline__ void zero_scan_stats(const DMap& M, int zero_stats) {
+  if (zero_stats && blockIdx.x == 0 && threadIdx.x < S_COUNT)
+    reinterpret_cast<unsigned long long*>(M.ctr + C_STATS)[threadIdx.x] = 0ull;
+}
+
 template <typename PT>
 __global__ void k_endpoints(DMap M, const uint8_t* __restrict__ pts, size_t stride, uint32_t n,
                             double fx, double fy, double fz, double max_range, double mr2,
                             double inv_res, int keep_nonfinite, int4* __restrict__ ep,
-                            uint4* tab, uint32_t tmask) {
+                            uint4* tab, uint32_t tmask, int zero_stats) {
+  zero_scan_stats(M, zero_stats);
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   int4 e = make_int4(0, 0, 0, EP_SKIP);
   if (i < n) {
@@ -71,7 +78,9 @@ __device__ __forceinline__ float xf_row(const Xf& t, int r, float x, float y, fl
 __global__ void k_endpoints_sensor(DMap M, const uint8_t* __restrict__ pts, size_t stride,
                                    uint32_t n, Xf xf, double fx, double fy, double fz,
                                    double max_range, double mr2, double inv_res,
-                                   int4* __restrict__ ep, uint4* tab, uint32_t tmask) {
+                                   int4* __restrict__ ep, uint4* tab, uint32_t tmask,
+                                   int zero_stats) {
+  zero_scan_stats(M, zero_stats);
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float* p = reinterpret_cast<const float*>(pts + size_t(i) * stride);
@@ -103,9 +112,13 @@ __global__ void k_endpoints_kind(DMap M, const double* __restrict__ pts, uint32_
 
 // The lowest-index point of each endpoint cell decides and applies
 // (winner_apply) and, if its ray is cast, joins the ray list.
-__global__ void k_winners(DMap M, const int4* __restrict__ ep, uint32_t n,
+// One block-wide atomic each for the ray list, the point count and the ray
+// lengths (a per-warp atomic on three shared counters serialised in L2).
+__global__ void __launch_bounds__(256) k_winners(DMap M, const int4* __restrict__ ep, uint32_t n,
                           const uint4* __restrict__ tab, uint32_t tmask, int ox, int oy, int oz,
                           int32_t u, Opts o, int4* __restrict__ cast, uint32_t cast_cap) {
+  __shared__ uint32_t s_cnt[8], s_pts[8], s_base;
+  __shared__ unsigned long long s_len[8];
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   bool add = false;
   int4 e = make_int4(0, 0, 0, EP_SKIP);
@@ -115,21 +128,36 @@ __global__ void k_winners(DMap M, const int4* __restrict__ ep, uint32_t n,
       if (dedup_lookup(tab, tmask, e.x, e.y, e.z) == i) add = winner_apply(M, e, u, o);
     }
   }
-  const unsigned lane = threadIdx.x & 31;
+  const unsigned lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const unsigned valid = __ballot_sync(0xffffffffu, i < n && e.w != EP_SKIP);
   const unsigned am = __ballot_sync(0xffffffffu, add);
-  unsigned long long len = add ? chebyshev(ox, oy, oz, e.x, e.y, e.z) : 0;
-  len = __reduce_add_sync(0xffffffffu, static_cast<unsigned>(len));
-  uint32_t base = 0;
+  const uint32_t len = add ? chebyshev(ox, oy, oz, e.x, e.y, e.z) : 0u;
+  const unsigned long long wlen = __reduce_add_sync(0xffffffffu, len >> 16) * 65536ull +
+                                  __reduce_add_sync(0xffffffffu, len & 0xFFFFu);
   if (lane == 0) {
-    unsigned long long* st = reinterpret_cast<unsigned long long*>(M.ctr + C_STATS);
-    if (valid) atomicAdd(st + S_POINTS, static_cast<unsigned long long>(__popc(valid)));
-    if (len) atomicAdd(st + S_RAY_LEN, len);
-    if (am) base = atomicAdd(M.ctr + C_CAST, static_cast<uint32_t>(__popc(am)));
+    s_cnt[wid] = __popc(am);
+    s_pts[wid] = __popc(valid);
+    s_len[wid] = wlen;
   }
-  base = __shfl_sync(0xffffffffu, base, 0);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t tot = 0, pts = 0;
+    unsigned long long tl = 0;
+    for (unsigned w = 0; w < blockDim.x / 32; w++) {
+      const uint32_t c = s_cnt[w];
+      s_cnt[w] = tot;
+      tot += c;
+      pts += s_pts[w];
+      tl += s_len[w];
+    }
+    unsigned long long* st = reinterpret_cast<unsigned long long*>(M.ctr + C_STATS);
+    if (pts) atomicAdd(st + S_POINTS, static_cast<unsigned long long>(pts));
+    if (tl) atomicAdd(st + S_RAY_LEN, tl);
+    s_base = tot ? atomicAdd(M.ctr + C_CAST, tot) : 0u;
+  }
+  __syncthreads();
   if (add) {
-    const uint32_t k = base + __popc(am & ((1u << lane) - 1));
+    const uint32_t k = s_base + s_cnt[wid] + __popc(am & ((1u << lane) - 1));
     if (k < cast_cap)
       cast[k] = e;
     else
@@ -162,10 +190,15 @@ __global__ void k_apply(DMap M, const int4* __restrict__ cast, uint32_t cast_cap
 
 // Ray phase: one group of W lanes per listed ray (walk_ray, or walk_ray2 with
 // two cells per lane per step when U == 2).
+// Also clears tab[0, tab_n), the endpoint dedup table of the scan, so that
+// the next scan's endpoint phase starts from an empty table without a memset.
 template <int W, int U>
 __global__ void __launch_bounds__(256, U == 2 ? 3 : 4) k_rays(DMap M, const int4* __restrict__ cast,
                                                  uint32_t cast_cap, int ox, int oy, int oz,
-                                                 int32_t u, int32_t miss, int32_t cmin) {
+                                                 int32_t u, int32_t miss, int32_t cmin,
+                                                 uint4* __restrict__ tab, uint32_t tab_n) {
+  for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < tab_n; t += gridDim.x * blockDim.x)
+    tab[t] = make_uint4(kNone, kNone, kNone, kNone);
   const uint32_t n_cast = min(ld_volatile(M.ctr + C_CAST), cast_cap);
   const unsigned lane = threadIdx.x & 31;
   const unsigned sl = lane & (W - 1);
@@ -283,11 +316,15 @@ int endpoint_phase(bxg_pmap_s* pm, uint32_t n, int ox, int oy, int oz, Launch&& 
   MapCore* m = &pm->core;
   const uint32_t tcap = next_pow2(uint64_t(n) * 2);
   BXG_CUDA(m, m->s_ep.ensure(size_t(n) * 16));
+  const void* old_tab = m->s_dedup.p;
   BXG_CUDA(m, m->s_dedup.ensure(size_t(tcap) * 16));
+  if (m->s_dedup.p != old_tab) m->dedup_clean = 0;
   // the ray list persists across add-batches until updateFreeCells
   const uint64_t need = pm->cast_ub + n;
   BXG_CUDA(m, m->s_cast.ensure_keep(need * 16, pm->cast_ub * 16, m->stream));
-  launch_dedup_clear(m, m->s_dedup.as<uint4>(), tcap);
+  if (m->dedup_clean < tcap) launch_dedup_clear(m, m->s_dedup.as<uint4>(), tcap);
+  m->dedup_clean = 0;
+  m->dedup_used = std::max(m->dedup_used, tcap);
   const unsigned blocks = (n + 255) / 256;
   launch_ep(blocks, m->s_ep.as<int4>(), m->s_dedup.as<uint4>(), tcap - 1);
   BXG_LAUNCHED(m);
@@ -329,17 +366,21 @@ int launch_rays(bxg_pmap_s* pm, int ox, int oy, int oz) {
   const dim3 g{unsigned(blocks)}, b{unsigned(bs)};
   const int4* c = m->s_cast.as<int4>();
   const int32_t uc = pm->update_count;
+  uint4* const tab = m->s_dedup.as<uint4>();
+  const uint32_t tab_n = m->dedup_used;
   if (rpw == 4) {
-    if (u2) k_rays<8, 2><<<g, b, 0, m->stream>>>(m->dm, c, ccap, ox, oy, oz, uc, o.miss, o.cmin);
-    else k_rays<8, 1><<<g, b, 0, m->stream>>>(m->dm, c, ccap, ox, oy, oz, uc, o.miss, o.cmin);
+    if (u2) k_rays<8, 2><<<g, b, 0, m->stream>>>(m->dm, c, ccap, ox, oy, oz, uc, o.miss, o.cmin, tab, tab_n);
+    else k_rays<8, 1><<<g, b, 0, m->stream>>>(m->dm, c, ccap, ox, oy, oz, uc, o.miss, o.cmin, tab, tab_n);
   } else if (rpw == 2) {
-    if (u2) k_rays<16, 2><<<g, b, 0, m->stream>>>(m->dm, c, ccap, ox, oy, oz, uc, o.miss, o.cmin);
-    else k_rays<16, 1><<<g, b, 0, m->stream>>>(m->dm, c, ccap, ox, oy, oz, uc, o.miss, o.cmin);
+    if (u2) k_rays<16, 2><<<g, b, 0, m->stream>>>(m->dm, c, ccap, ox, oy, oz, uc, o.miss, o.cmin, tab, tab_n);
+    else k_rays<16, 1><<<g, b, 0, m->stream>>>(m->dm, c, ccap, ox, oy, oz, uc, o.miss, o.cmin, tab, tab_n);
   } else {
-    if (u2) k_rays<32, 2><<<g, b, 0, m->stream>>>(m->dm, c, ccap, ox, oy, oz, uc, o.miss, o.cmin);
-    else k_rays<32, 1><<<g, b, 0, m->stream>>>(m->dm, c, ccap, ox, oy, oz, uc, o.miss, o.cmin);
+    if (u2) k_rays<32, 2><<<g, b, 0, m->stream>>>(m->dm, c, ccap, ox, oy, oz, uc, o.miss, o.cmin, tab, tab_n);
+    else k_rays<32, 1><<<g, b, 0, m->stream>>>(m->dm, c, ccap, ox, oy, oz, uc, o.miss, o.cmin, tab, tab_n);
   }
   BXG_LAUNCHED(m);
+  m->dedup_clean = std::max(m->dedup_clean, tab_n);
+  m->dedup_used = 0;
   return BXG_OK;
 }
 
@@ -427,8 +468,10 @@ int insert_impl(bxg_pmap m_, const PT* xyz, size_t stride, size_t n, const PT* o
                         std::max<size_t>(n / 64, 256));
   if (st) return st;
   record(pm, 0);  // the scan's device time starts here
-  st = reset_scan_stats(m);
-  if (st) return st;
+  if (!n) {  // otherwise the endpoint kernel zeroes the statistics
+    st = reset_scan_stats(m);
+    if (st) return st;
+  }
   if (n) {
     const void* dpts = nullptr;
     st = stage_in(m, m->s_in, xyz, stride * (n - 1) + 3 * sizeof(PT), &dpts);
@@ -440,11 +483,11 @@ int insert_impl(bxg_pmap m_, const PT* xyz, size_t stride, size_t n, const PT* o
                           if (xf)
                             k_endpoints_sensor<<<blocks, 256, 0, m->stream>>>(
                                 m->dm, static_cast<const uint8_t*>(dpts), stride, uint32_t(n),
-                                *xf, fx, fy, fz, max_range, mr2, m->inv_res, ep, tab, tmask);
+                                *xf, fx, fy, fz, max_range, mr2, m->inv_res, ep, tab, tmask, 1);
                           else
                             k_endpoints<PT><<<blocks, 256, 0, m->stream>>>(
                                 m->dm, static_cast<const uint8_t*>(dpts), stride, uint32_t(n), fx,
-                                fy, fz, max_range, mr2, m->inv_res, keep, ep, tab, tmask);
+                                fy, fz, max_range, mr2, m->inv_res, keep, ep, tab, tmask, 1);
                         });
     if (st) return st;
   }
@@ -629,7 +672,7 @@ int pmap_complete_scan(bxg_pmap_s* pm, const int4* d_cast, const uint32_t* d_cou
     BXG_LAUNCHED(m);
     const unsigned rblocks = unsigned(std::min<uint64_t>((cap + 7) / 8, uint64_t(m->sm_count) * 8));
     k_rays<32, 1><<<std::max(rblocks, 1u), 256, 0, m->stream>>>(m->dm, d_cast, cap, ox, oy, oz,
-                                                               u, o.miss, o.cmin);
+                                                               u, o.miss, o.cmin, nullptr, 0);
     BXG_LAUNCHED(m);
     st = core_sync(m, &err);
     if (st && !(err & (ERR_POOL_INNER | ERR_POOL_LEAF | ERR_HASH_FULL))) return st;

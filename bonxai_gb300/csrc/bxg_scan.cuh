@@ -127,7 +127,9 @@ __device__ __forceinline__ bool winner_apply(const DMap& M, int4 e, int32_t u, c
 // lanes of one step touch a few leaves: the first lane of each leaf run (a
 // "head") looks the leaf up -- inline fast path first, the bounded-wait
 // creation path only on a miss -- and the others take its slot by shuffle.
-// The group carries the last leaf and the last root between steps.
+// The group carries the last leaf between steps. Heads probe the root hash
+// directly: neighbouring heads hit the same buckets in L1, and carrying the
+// last root through the group cost more shuffles than the probes it saved.
 //
 // Leaf runs are found by comparing a 30-bit packed leaf index (10 low bits per
 // axis): two cells at most W+1 steps apart on one ray are at most a few
@@ -166,8 +168,6 @@ __device__ __forceinline__ void walk_ray_op(const DMap& M, int4 e, int ox, int o
   axis_init(Z, az, m, two_m, rtm, sl, W);
   uint32_t pkey = kNone;  // packed leaf index of the previous step's last lane
   uint32_t pleaf = kNone;
-  int rkx = kEmptyKey, rky = kEmptyKey, rkz = kEmptyKey;  // group's last root
-  uint32_t rin = kNone;
 
   for (uint32_t base = 0; base < m; base += W) {
     const bool act = base + sl < m;
@@ -180,17 +180,11 @@ __device__ __forceinline__ void walk_ray_op(const DMap& M, int4 e, int ox, int o
     uint32_t q = __shfl_up_sync(gmask, key, 1, W);
     if (sl == 0) q = pkey;
     const bool head = act && key != q;
-    uint32_t leaf = kNone, in = kNone;
-    bool root_miss = false;
+    uint32_t leaf = kNone;
     if (head) {
       const int rx = cx & rm, ry = cy & rm, rz = cz & rm;
-      if (rx == rkx && ry == rky && rz == rkz) {
-        in = rin;
-      } else {
-        root_miss = true;
-        in = root_probe_fast(M, rx, ry, rz);
-        if (in == kPending) in = root_get_or_create(M, rx, ry, rz);
-      }
+      uint32_t in = root_probe_fast(M, rx, ry, rz);
+      if (in == kPending) in = root_get_or_create(M, rx, ry, rz);
       if (in != kNone) {
         const uint32_t ii = inner_index(M, cx, cy, cz);
         leaf = M.ichild[static_cast<size_t>(in) * M.isize + ii];
@@ -204,14 +198,6 @@ __device__ __forceinline__ void walk_ray_op(const DMap& M, int4 e, int ox, int o
     const unsigned below = hm & ((2u << sl) - 1u);
     const uint32_t got = __shfl_sync(gmask, leaf, below ? 31 - __clz(below) : 0, W);
     leaf = below ? got : pleaf;
-    const unsigned rmiss = (__ballot_sync(gmask, root_miss) & gmask) >> gbase;
-    if (rmiss) {  // remember the root of the highest head that probed the hash
-      const int hl = 31 - __clz(rmiss);
-      rkx = __shfl_sync(gmask, cx & rm, hl, W);
-      rky = __shfl_sync(gmask, cy & rm, hl, W);
-      rkz = __shfl_sync(gmask, cz & rm, hl, W);
-      rin = __shfl_sync(gmask, in, hl, W);
-    }
     op(act, leaf, leaf_index(M, cx, cy, cz), base + sl);
     const uint32_t rem = m - base;
     const int last = static_cast<int>(rem < W ? rem : W) - 1;
@@ -245,19 +231,13 @@ __device__ __forceinline__ void walk_ray(const DMap& M, int4 e, int ox, int oy, 
                  });
 }
 
-// Leaf slot of a head cell: the group's cached root when it matches, else the
-// inline hash probe, else the bounded-wait creation path.
-__device__ __forceinline__ uint32_t head_leaf(const DMap& M, int cx, int cy, int cz, int32_t rm,
-                                              int rkx, int rky, int rkz, uint32_t rin,
-                                              uint32_t& in, bool& root_miss) {
+// Leaf slot of a head cell: the inline hash probe, else the bounded-wait
+// creation path.
+__device__ __forceinline__ uint32_t head_leaf(const DMap& M, int cx, int cy, int cz,
+                                              int32_t rm) {
   const int rx = cx & rm, ry = cy & rm, rz = cz & rm;
-  if (rx == rkx && ry == rky && rz == rkz) {
-    in = rin;
-  } else {
-    root_miss = true;
-    in = root_probe_fast(M, rx, ry, rz);
-    if (in == kPending) in = root_get_or_create(M, rx, ry, rz);
-  }
+  uint32_t in = root_probe_fast(M, rx, ry, rz);
+  if (in == kPending) in = root_get_or_create(M, rx, ry, rz);
   if (in == kNone) return kNone;
   const uint32_t ii = inner_index(M, cx, cy, cz);
   uint32_t leaf = M.ichild[static_cast<size_t>(in) * M.isize + ii];
@@ -307,8 +287,6 @@ __device__ __forceinline__ void walk_ray2(const DMap& M, int4 e, int ox, int oy,
   axis_init(Y, ay, m, two_m, rtm, sl, W);
   axis_init(Z, az, m, two_m, rtm, sl, W);
   uint32_t pkey = kNone, pleaf = kNone;
-  int rkx = kEmptyKey, rky = kEmptyKey, rkz = kEmptyKey;
-  uint32_t rin = kNone;
 
   for (uint32_t base = 0; base < m; base += 2 * W) {
     uint32_t nx2, rx2, ny2, ry2, nz2, rz2;
@@ -334,10 +312,9 @@ __device__ __forceinline__ void walk_ray2(const DMap& M, int4 e, int ox, int oy,
       q2 = last1;
     }
     const bool head1 = act1 && key1 != q1, head2 = act2 && key2 != q2;
-    uint32_t leaf1 = kNone, leaf2 = kNone, in1 = kNone, in2 = kNone;
-    bool miss1 = false, miss2 = false;
-    if (head1) leaf1 = head_leaf(M, c1x, c1y, c1z, rm, rkx, rky, rkz, rin, in1, miss1);
-    if (head2) leaf2 = head_leaf(M, c2x, c2y, c2z, rm, rkx, rky, rkz, rin, in2, miss2);
+    uint32_t leaf1 = kNone, leaf2 = kNone;
+    if (head1) leaf1 = head_leaf(M, c1x, c1y, c1z, rm);
+    if (head2) leaf2 = head_leaf(M, c2x, c2y, c2z, rm);
     const unsigned hm1 = (__ballot_sync(gmask, head1) & gmask) >> gbase;
     const unsigned hm2 = (__ballot_sync(gmask, head2) & gmask) >> gbase;
     const unsigned below1 = hm1 & ((2u << sl) - 1u), below2 = hm2 & ((2u << sl) - 1u);
@@ -346,18 +323,6 @@ __device__ __forceinline__ void walk_ray2(const DMap& M, int4 e, int ox, int oy,
     const uint32_t end1 = __shfl_sync(gmask, leaf1, W - 1, W);
     const uint32_t g2 = __shfl_sync(gmask, leaf2, below2 ? 31 - __clz(below2) : 0, W);
     leaf2 = below2 ? g2 : end1;
-    const unsigned rm2 = (__ballot_sync(gmask, miss2) & gmask) >> gbase;
-    const unsigned rm1 = (__ballot_sync(gmask, miss1) & gmask) >> gbase;
-    if (rm2 | rm1) {  // remember the root of the furthest head that probed the hash
-      const bool two = rm2 != 0;
-      const int hl = 31 - __clz(two ? rm2 : rm1);
-      const int hx = two ? c2x : c1x, hy = two ? c2y : c1y, hz = two ? c2z : c1z;
-      const uint32_t hin = two ? in2 : in1;
-      rkx = __shfl_sync(gmask, hx & rm, hl, W);
-      rky = __shfl_sync(gmask, hy & rm, hl, W);
-      rkz = __shfl_sync(gmask, hz & rm, hl, W);
-      rin = __shfl_sync(gmask, hin, hl, W);
-    }
     const bool do1 = act1 && leaf1 != kNone, do2 = act2 && leaf2 != kNone;
     int32_t* cp1 = cells + static_cast<size_t>(do1 ? leaf1 : 0) * M.lsize +
                    leaf_index(M, c1x, c1y, c1z);

@@ -70,6 +70,38 @@ def test_lidar_scans_vs_oracle(gpu, port, rpw, unroll):
     assert_same_map(m, o)
 
 
+def test_scans_interleaved_with_grid_writes_and_added_points(gpu, port):
+    """Scans share a scratch table with the grid-view batch calls and with
+    addHitPoint/addMissPoint batches (the ray kernel leaves it empty for the
+    next scan); interleaving all three must not change any result."""
+    scene = synth.LidarScene()
+    m = gpu.ProbabilisticMap(0.1)
+    o = port.pmap(0.1)
+    lib = gpu.load_library()
+    rng = np.random.default_rng(12)
+    for k in range(5):
+        pts, org = scene.scan(k, n_points=20000 + 3000 * k)
+        assert m.insert_point_cloud(pts, org, 30.0) == o.insert(pts, org, 30.0)
+        if k % 2 == 0:
+            # rewrite a third of the cells with their own words: the map is
+            # unchanged, the scratch table is not
+            xyz, cells = m.dump()
+            c = np.ascontiguousarray(xyz[::3])
+            w = np.ascontiguousarray(cells[::3])
+            assert lib.bxg_grid_set_values(lib.bxg_pmap_grid(m.h), c.ctypes.data, w.ctypes.data,
+                                           len(c), None) == 0
+        else:
+            h = (org + rng.normal(0, 3, (500, 3))).astype(np.float64)
+            mi = (org + rng.normal(0, 3, (300, 3))).astype(np.float64)
+            m.add_hit_points(h)
+            o.add_hit(h)
+            m.add_miss_points(mi)
+            o.add_miss(mi)
+            assert m.update_free_cells(org.astype(np.float64)) == o.update_free_cells(
+                org.astype(np.float64))
+    assert_same_map(m, o)
+
+
 def test_depth_frames_vs_oracle(gpu, port):
     room = synth.DepthRoom()
     m = gpu.ProbabilisticMap(room.resolution)
