@@ -45,6 +45,7 @@ constexpr size_t kMetaBytes = kOffPrefix + (kMaxTickScans + 1) * 4;
 struct TickScan {
   DMap M;
   double fx, fy, fz, max_range, mr2, inv_res;
+  EpFast fast;                   // float filter of the endpoint math
   int32_t ox, oy, oz, u;
   Opts o;
   unsigned long long pt_begin;   // first point of this scan in the tick's arrays
@@ -54,6 +55,8 @@ struct TickScan {
   int32_t keep_nonfinite;
   int32_t pad;
 };
+
+static_assert(sizeof(TickScan) % 8 == 0, "TickScan is copied to shared memory in 8-byte words");
 
 struct TickArgs {
   const uint8_t* pts;  // packed float xyz of all scans
@@ -171,7 +174,7 @@ __global__ void __launch_bounds__(256, U == 2 ? 3 : 4) k_tick(const TickArgs* __
     const TickScan& S = sc[s];
     const float* p = reinterpret_cast<const float*>(A.pts) + 3 * i;
     const int4 e = compute_endpoint<float>(p, S.fx, S.fy, S.fz, S.max_range, S.mr2, S.inv_res,
-                                           S.keep_nonfinite != 0);
+                                           S.keep_nonfinite != 0, &S.fast);
     A.ep[i] = e;
     if (e.w != EP_SKIP)
       dedup_min_insert(A.tab + S.tab_begin, S.tmask, e.x, e.y, e.z,
@@ -543,6 +546,7 @@ int bxg_batch_insert_f32(bxg_batch b, const bxg_pmap* maps, size_t n_scans, cons
     S.max_range = max_ranges[s];
     S.mr2 = max_ranges[s] * max_ranges[s];
     S.inv_res = pm->core.inv_res;
+    S.fast = make_ep_fast(S.fx, S.fy, S.fz, S.max_range, S.inv_res);
     S.ox = static_cast<int>(std::floor(S.fx * pm->core.inv_res));
     S.oy = static_cast<int>(std::floor(S.fy * pm->core.inv_res));
     S.oz = static_cast<int>(std::floor(S.fz * pm->core.inv_res));

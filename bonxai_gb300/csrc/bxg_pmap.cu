@@ -27,23 +27,28 @@
 namespace bxg {
 
 // Endpoint of each point; lowest index per endpoint cell in the scratch table.
-// zero_stats: the scan's statistics start at zero (saves a memset).
-__device__ __forceinline__ void zero_scan_stats(const DMap& M, int zero_stats) {
-  if (zero_stats && blockIdx.x == 0 && threadIdx.x < S_COUNT)
+// zero: bit 0 -- the scan's statistics start at zero; bit 1 -- the ray list
+// starts empty (no rays queued by earlier addHitPoint/addMissPoint batches).
+// Done by the first kernel of a scan instead of memsets.
+enum : int { ZERO_STATS = 1, ZERO_CAST = 2 };
+__device__ __forceinline__ void zero_scan_stats(const DMap& M, int zero) {
+  if (blockIdx.x != 0) return;
+  if ((zero & ZERO_STATS) && threadIdx.x < S_COUNT)
     reinterpret_cast<unsigned long long*>(M.ctr + C_STATS)[threadIdx.x] = 0ull;
+  if ((zero & ZERO_CAST) && threadIdx.x == 32) M.ctr[C_CAST] = 0u;
 }
 
 template <typename PT>
 __global__ void k_endpoints(DMap M, const uint8_t* __restrict__ pts, size_t stride, uint32_t n,
                             double fx, double fy, double fz, double max_range, double mr2,
                             double inv_res, int keep_nonfinite, int4* __restrict__ ep,
-                            uint4* tab, uint32_t tmask, int zero_stats) {
+                            uint4* tab, uint32_t tmask, int zero_stats, EpFast F) {
   zero_scan_stats(M, zero_stats);
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   int4 e = make_int4(0, 0, 0, EP_SKIP);
   if (i < n) {
     const PT* p = reinterpret_cast<const PT*>(pts + size_t(i) * stride);
-    e = compute_endpoint<PT>(p, fx, fy, fz, max_range, mr2, inv_res, keep_nonfinite != 0);
+    e = compute_endpoint<PT>(p, fx, fy, fz, max_range, mr2, inv_res, keep_nonfinite != 0, &F);
   }
   // Neighbouring points often share an endpoint cell: within a warp only the
   // lowest lane (lowest index) of each cell enters the table; the others can
@@ -79,7 +84,7 @@ __global__ void k_endpoints_sensor(DMap M, const uint8_t* __restrict__ pts, size
                                    uint32_t n, Xf xf, double fx, double fy, double fz,
                                    double max_range, double mr2, double inv_res,
                                    int4* __restrict__ ep, uint4* tab, uint32_t tmask,
-                                   int zero_stats) {
+                                   int zero_stats, EpFast F) {
   zero_scan_stats(M, zero_stats);
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -90,7 +95,7 @@ __global__ void k_endpoints_sensor(DMap M, const uint8_t* __restrict__ pts, size
     return;
   }
   const float w[3] = {xf_row(xf, 0, x, y, z), xf_row(xf, 1, x, y, z), xf_row(xf, 2, x, y, z)};
-  const int4 e = compute_endpoint<float>(w, fx, fy, fz, max_range, mr2, inv_res, true);
+  const int4 e = compute_endpoint<float>(w, fx, fy, fz, max_range, mr2, inv_res, true, &F);
   ep[i] = e;
   if (e.w != EP_SKIP) dedup_min_insert(tab, tmask, e.x, e.y, e.z, i, M);
 }
@@ -99,7 +104,8 @@ __global__ void k_endpoints_sensor(DMap M, const uint8_t* __restrict__ pts, size
 // per-point kind (0 hit, 1 miss) when kinds != nullptr.
 __global__ void k_endpoints_kind(DMap M, const double* __restrict__ pts, uint32_t n, int kind,
                                  const uint8_t* __restrict__ kinds, double inv_res,
-                                 int4* __restrict__ ep, uint4* tab, uint32_t tmask) {
+                                 int4* __restrict__ ep, uint4* tab, uint32_t tmask, int zero) {
+  zero_scan_stats(M, zero);
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   if (kinds) kind = kinds[i] ? EP_MISS : EP_HIT;
@@ -416,7 +422,7 @@ int finish_scan(bxg_pmap_s* pm, int ox, int oy, int oz, bool cast_rays, uint64_t
   if (st) return st;
   const unsigned long long* hs = reinterpret_cast<const unsigned long long*>(m->h_ctr + C_STATS);
   pm->last_stats[0] = hs[S_POINTS];
-  pm->last_stats[1] = m->h_ctr[C_CAST];
+  pm->last_stats[1] = pm->cast_ub ? m->h_ctr[C_CAST] : 0;
   pm->last_stats[2] = hs[S_VISITED];
   pm->last_stats[3] = hs[S_UPDATED];
   pm->last_stats[4] = m->h_ctr[C_LEAF];
@@ -430,11 +436,10 @@ int finish_scan(bxg_pmap_s* pm, int ox, int oy, int oz, bool cast_rays, uint64_t
     }
   }
   if (cast_rays) {
-    // end of scan: empty the ray list, advance the counter (cpp:301-310)
-    BXG_CUDA(m, cudaMemsetAsync(m->ctr.as<uint32_t>() + C_CAST, 0, 4, m->stream));
+    // end of scan: empty the ray list (the next scan's first kernel zeroes
+    // the device count), advance the counter (cpp:301-310)
     pm->cast_ub = 0;
     if (++pm->update_count == 4) pm->update_count = 1;
-    BXG_CUDA(m, cudaStreamSynchronize(m->stream));
   }
   return core_maintain(m);
 }
@@ -478,16 +483,21 @@ int insert_impl(bxg_pmap m_, const PT* xyz, size_t stride, size_t n, const PT* o
     if (st) return st;
     const double mr2 = max_range * max_range;
     const int keep = (m->flags & BXG_FLAG_KEEP_NONFINITE) ? 1 : 0;
+    const int zero = ZERO_STATS | (pm->cast_ub == 0 ? ZERO_CAST : 0);
+    EpFast fast = make_ep_fast(fx, fy, fz, max_range, m->inv_res);
+    if (sizeof(PT) != 4) fast.on = 0;
     st = endpoint_phase(pm, uint32_t(n), o[0], o[1], o[2],
                         [&](unsigned blocks, int4* ep, uint4* tab, uint32_t tmask) {
                           if (xf)
                             k_endpoints_sensor<<<blocks, 256, 0, m->stream>>>(
                                 m->dm, static_cast<const uint8_t*>(dpts), stride, uint32_t(n),
-                                *xf, fx, fy, fz, max_range, mr2, m->inv_res, ep, tab, tmask, 1);
+                                *xf, fx, fy, fz, max_range, mr2, m->inv_res, ep, tab, tmask, zero,
+                                fast);
                           else
                             k_endpoints<PT><<<blocks, 256, 0, m->stream>>>(
                                 m->dm, static_cast<const uint8_t*>(dpts), stride, uint32_t(n), fx,
-                                fy, fz, max_range, mr2, m->inv_res, keep, ep, tab, tmask, 1);
+                                fy, fz, max_range, mr2, m->inv_res, keep, ep, tab, tmask, zero,
+                                fast);
                         });
     if (st) return st;
   }
@@ -515,10 +525,8 @@ int add_points(bxg_pmap m_, const double* xyz, size_t n, int kind,
   if (!xyz || n >= 0x7FFFFFFFu) return set_error(m, BXG_ERR_INVALID_ARG, "null input");
   cudaSetDevice(m->device);
   record(pm, 0);
-  if (pm->cast_ub == 0) {
-    int st = reset_scan_stats(m);
-    if (st) return st;
-  }
+  // the first batch after a scan starts the statistics and the ray list
+  const int zero = pm->cast_ub == 0 ? (ZERO_STATS | ZERO_CAST) : 0;
   const void* dpts = nullptr;
   const void* dkinds = nullptr;
   int st = stage_in(m, m->s_in, xyz, n * 24, &dpts);
@@ -531,7 +539,8 @@ int add_points(bxg_pmap m_, const double* xyz, size_t n, int kind,
                       [&](unsigned blocks, int4* ep, uint4* tab, uint32_t tmask) {
                         k_endpoints_kind<<<blocks, 256, 0, m->stream>>>(
                             m->dm, static_cast<const double*>(dpts), uint32_t(n), kind,
-                            static_cast<const uint8_t*>(dkinds), m->inv_res, ep, tab, tmask);
+                            static_cast<const uint8_t*>(dkinds), m->inv_res, ep, tab, tmask,
+                            zero);
                       });
   if (st) return st;
   // apply now so that queries see the endpoint updates, as in the reference
@@ -798,7 +807,7 @@ int bxg_pmap_update_free_cells(bxg_pmap pm, const double origin[3], uint64_t* ra
     int st = core_sync(m);
     if (st) return st;
   }
-  const uint32_t n_cast = m->h_ctr[C_CAST];
+  const uint32_t n_cast = pm->cast_ub ? m->h_ctr[C_CAST] : 0;  // the device count is stale
   uint64_t len = 0;
   if (ray_cells && n_cast) {
     std::vector<int4> h(n_cast);

@@ -21,6 +21,8 @@
 //    conditional store suffice.
 #pragma once
 
+#include <cmath>
+
 #include "bxg_device.cuh"
 
 namespace bxg {
@@ -61,16 +63,126 @@ __device__ __forceinline__ uint32_t dedup_lookup(const uint4* tab, uint32_t tmas
   return kNone;
 }
 
+// float32 filter for the endpoint math of float clouds. GB300 runs double
+// precision at a small fraction of its float rate, and the double math was the
+// bound of the endpoint kernel (fp64 pipe 60 % busy). Each point is first
+// computed in float with a bound on its distance from the double result; a
+// result that no error within the bound can change -- the hit/miss test
+// decided with margin, every floor() at least the bound away from an integer
+// -- is exact, and any other point goes through the double path unchanged
+// (an adaptive-precision filter in the manner of Shewchuk's predicates).
+//
+// Bounds, with u = 2^-24 and all float operations rounded to nearest:
+//   sq:  |sq_f - sq| <= 5u sq               (vx, vy, vz exact in double or
+//                                           within u; three products, two sums)
+//   hit: |y_f - y_d| <= 2u |y|              (inv_res rounded to float, one product)
+//   miss: |y_f - y_d| <= ((7.5 mr + |e|) inv_res + 2 |y|) u
+//        (sqrt 3.5u, quotient 5.5u, times max_range 7.5u, plus origin, times inv_res)
+// The filter uses margins four times these bounds.
+struct EpFast {
+  float ox, oy, oz;    // origin (exactly the double origin)
+  float inv_res;       // 1 / resolution rounded to float
+  float mr;            // max_range rounded to float
+  float sq_hi, sq_lo;  // sq_f above sq_hi: miss; below sq_lo: hit; else double path
+  int on;              // the filter applies (float origin, finite parameters)
+};
+
+inline EpFast make_ep_fast(double fx, double fy, double fz, double max_range, double inv_res) {
+  EpFast F{};
+  F.ox = static_cast<float>(fx);
+  F.oy = static_cast<float>(fy);
+  F.oz = static_cast<float>(fz);
+  F.inv_res = static_cast<float>(inv_res);
+  F.mr = static_cast<float>(max_range);
+  const double mr2 = max_range * max_range;
+  const double hi = mr2 * (1.0 + 0x1p-19), lo = mr2 * (1.0 - 0x1p-19);
+  F.sq_hi = std::nextafter(static_cast<float>(hi), HUGE_VALF);
+  F.sq_lo = std::nextafter(static_cast<float>(lo), 0.0f);
+  F.on = static_cast<double>(F.ox) == fx && static_cast<double>(F.oy) == fy &&
+         static_cast<double>(F.oz) == fz && std::isfinite(F.inv_res) && F.inv_res > 0.0f &&
+         !std::isnan(max_range) && max_range >= 0.0 &&
+         (std::isinf(max_range) || max_range < 1e30);
+  if (std::isinf(max_range)) F.sq_hi = F.sq_lo = HUGE_VALF;
+  return F;
+}
+
+// floor(y) when y is more than tol from an integer (and |y| < 2^23, where the
+// fractional part of a float is exact).
+__device__ __forceinline__ bool floor_filtered(float y, float tol, int& c) {
+  if (!(fabsf(y) < 8388608.0f)) return false;
+  const float fl = floorf(y);
+  if (__fsub_rn(y, fl) <= tol || __fsub_rn(__fadd_rn(fl, 1.0f), y) <= tol) return false;
+  c = static_cast<int>(fl);
+  return true;
+}
+
+// The float filter for one finite point; false = use the double path.
+__device__ __forceinline__ bool endpoint_fast(float px, float py, float pz, const EpFast& F,
+                                              int4& out) {
+  const float vx = __fsub_rn(px, F.ox), vy = __fsub_rn(py, F.oy), vz = __fsub_rn(pz, F.oz);
+  const float sq = __fadd_rn(__fadd_rn(__fmul_rn(vx, vx), __fmul_rn(vy, vy)), __fmul_rn(vz, vz));
+  if (!(sq < 1e30f)) return false;
+  float ex, ey, ez, tx, ty, tz;
+  int kind;
+  if (sq < F.sq_lo) {
+    ex = px;
+    ey = py;
+    ez = pz;
+    kind = EP_HIT;
+  } else if (sq > F.sq_hi) {
+    const float s = __fsqrt_rn(sq);
+    ex = __fadd_rn(F.ox, __fmul_rn(__fdiv_rn(vx, s), F.mr));
+    ey = __fadd_rn(F.oy, __fmul_rn(__fdiv_rn(vy, s), F.mr));
+    ez = __fadd_rn(F.oz, __fmul_rn(__fdiv_rn(vz, s), F.mr));
+    kind = EP_MISS;
+  } else {
+    return false;
+  }
+  const float yx = __fmul_rn(ex, F.inv_res), yy = __fmul_rn(ey, F.inv_res),
+              yz = __fmul_rn(ez, F.inv_res);
+  if (kind == EP_HIT) {  // 4 x 2u |y|
+    tx = fabsf(yx) * 4.76837158e-7f;
+    ty = fabsf(yy) * 4.76837158e-7f;
+    tz = fabsf(yz) * 4.76837158e-7f;
+  } else {  // 4 x ((7.5 mr + |e|) inv_res + 2 |y|) u, with 8 for 7.5
+    const float m8 = 8.0f * F.mr;
+    tx = ((m8 + fabsf(ex)) * F.inv_res + 2.0f * fabsf(yx)) * 2.38418579e-7f;
+    ty = ((m8 + fabsf(ey)) * F.inv_res + 2.0f * fabsf(yy)) * 2.38418579e-7f;
+    tz = ((m8 + fabsf(ez)) * F.inv_res + 2.0f * fabsf(yz)) * 2.38418579e-7f;
+  }
+  int cx, cy, cz;
+  // a hit coordinate that is exactly zero gives cell 0 in double as well (a
+  // miss coordinate rounded to zero in float need not be zero in double)
+  const bool hit = kind == EP_HIT;
+  if (hit && ex == 0.0f) cx = 0; else if (!floor_filtered(yx, tx, cx)) return false;
+  if (hit && ey == 0.0f) cy = 0; else if (!floor_filtered(yy, ty, cy)) return false;
+  if (hit && ez == 0.0f) cz = 0; else if (!floor_filtered(yz, tz, cz)) return false;
+  out = make_int4(cx, cy, cz, kind);
+  return true;
+}
+
 // insertPointCloud's per-point math (probabilistic_map.hpp:144-156) in double
 // with one IEEE rounding per operation and no contraction:
 //   v = to - from; sq = (vx*vx + vy*vy) + vz*vz;
 //   sq >= max_range^2 ? miss at from + (v / sqrt(sq)) * max_range : hit at to
 // then posToCoord = floor(p * inv_resolution) (bonxai.hpp:404-410).
+// Float clouds go through the float filter first when F is on.
 // Returns {cell, EP_HIT | EP_MISS | EP_SKIP}.
 template <typename PT>
 __device__ __forceinline__ int4 compute_endpoint(const PT* p, double fx, double fy, double fz,
                                                  double max_range, double mr2, double inv_res,
-                                                 bool keep_nonfinite) {
+                                                 bool keep_nonfinite,
+                                                 const EpFast* F = nullptr) {
+  if (sizeof(PT) == 4 && F && F->on) {
+    const float px = static_cast<float>(p[0]), py = static_cast<float>(p[1]),
+                pz = static_cast<float>(p[2]);
+    if (isfinite(px) && isfinite(py) && isfinite(pz)) {
+      int4 r;
+      if (endpoint_fast(px, py, pz, *F, r)) return r;
+    } else if (!keep_nonfinite) {
+      return make_int4(0, 0, 0, EP_SKIP);
+    }
+  }
   const double tx = static_cast<double>(p[0]), ty = static_cast<double>(p[1]),
                tz = static_cast<double>(p[2]);
   if (!keep_nonfinite && !finite3(tx, ty, tz)) return make_int4(0, 0, 0, EP_SKIP);

@@ -245,3 +245,59 @@ def test_kernel_timing_and_stats(gpu, port):
     assert st["points"] == 20000 and st["ray_cells_visited"] == v - 20000
     t = m.kernel_times()
     assert all(x >= 0 for x in t) and t[3] > 0
+
+
+def _adversarial_points(res, origin, max_range, n, seed):
+    """Points that sit on or within a few ulps of cell boundaries, and at
+    distances within a few ulps of max_range from the origin: the cases where
+    a float computation of the endpoint could round differently from the
+    reference's double computation."""
+    rng = np.random.default_rng(seed)
+    o = origin.astype(np.float64)
+    k = rng.integers(-400, 400, (n, 3)).astype(np.float64)
+    on_grid = (k * res).astype(np.float32)
+    ulps = rng.integers(-3, 4, (n, 3)).astype(np.float32)
+    toward = np.where(ulps < 0, -np.inf, np.inf).astype(np.float32)
+    near_grid = np.where(ulps == 0, on_grid, np.nextafter(on_grid, toward)).astype(np.float32)
+    d = rng.normal(size=(n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    scale = max_range * (1.0 + rng.integers(-8, 9, (n, 1)) * 2.0 ** -23)
+    near_range = (o + d * scale).astype(np.float32)
+    # misses whose endpoint lands near a cell boundary: directions toward grid points
+    tgt = (rng.integers(-300, 300, (n, 3)) * res).astype(np.float64)
+    dd = tgt - o
+    dd /= np.linalg.norm(dd, axis=1, keepdims=True)
+    far = (o + dd * (max_range * rng.uniform(1.0, 3.0, (n, 1)))).astype(np.float32)
+    zeros = near_grid.copy()
+    zeros[:, rng.integers(0, 3)] = 0.0
+    return np.concatenate([on_grid, near_grid, near_range, far, zeros])
+
+
+@pytest.mark.parametrize("res,origin,max_range", [
+    (0.1, np.array([0.0, 0.0, 0.0], np.float32), 30.0),
+    (0.1, np.array([1.25, -3.5, 1.7], np.float32), 30.0),
+    (0.05, np.array([0.3, 0.1, 0.0], np.float32), 12.5),
+    (0.02, np.array([-2.0, 4.0, 1.0], np.float32), 5.0),
+    (0.3, np.array([100.0, -50.0, 3.0], np.float32), 60.0),
+])
+def test_endpoint_filter_adversarial(gpu, port, res, origin, max_range):
+    """The float filter of the endpoint math falls back to double wherever the
+    result could differ: points on and next to cell boundaries and at max_range,
+    per map path and batched, bit-exact with the oracle."""
+    pts = _adversarial_points(res, origin, max_range, 4000, seed=int(res * 1000))
+    m = gpu.ProbabilisticMap(res)
+    o = port.pmap(res)
+    for k in range(3):
+        p = pts[k::3]
+        assert m.insert_point_cloud(p, origin, max_range) == o.insert(p, origin, max_range)
+    assert_same_map(m, o)
+    b = gpu.Batch()
+    bm = gpu.ProbabilisticMap(res)
+    o2 = port.pmap(res)
+    for k in range(3):
+        p = np.ascontiguousarray(pts[k::3])
+        rc = b.insert([bm], p, np.array([0, len(p)]), origin.reshape(1, 3), max_range)
+        assert rc[0] == o2.insert(p, origin, max_range)
+    bx_, bc = bm.dump()
+    ox, oc = o.dump()
+    assert np.array_equal(bx_, ox) and np.array_equal(bc, oc)
