@@ -664,6 +664,43 @@ def multimap_tick(specs, base, t):
     return scans
 
 
+def _mm_cpu_worker(job):
+    """One CPU process of the map-parallel baseline: inserts its maps' scans
+    with the oracle (single-threaded per map). Returns (ray cells, seconds)."""
+    from oracle import oracle as O
+    port = O.port()
+    V, dt = 0, 0.0
+    for res, pts, o in job:
+        m = port.pmap(res)
+        t0 = time.perf_counter()
+        V += m.insert(pts, o, MM_RANGE)
+        dt += time.perf_counter() - t0
+    return V, dt
+
+
+def mm_cpu_baseline(specs, scans, cores):
+    """The 64 maps' first tick on the host cores, maps spread over `cores`
+    processes (spawned: the GPU is already in use in this process)."""
+    import multiprocessing as mp
+    order = sorted(range(len(specs)), key=lambda i: -len(scans[i][0]))
+    jobs = [[] for _ in range(cores)]
+    load = [0] * cores
+    for i in order:  # longest first onto the least-loaded process
+        k = min(range(cores), key=lambda c: load[c])
+        jobs[k].append((specs[i].resolution, scans[i][0], scans[i][1]))
+        load[k] += len(scans[i][0])
+    with mp.get_context("spawn").Pool(cores) as pool:
+        t0 = time.perf_counter()
+        res = pool.map(_mm_cpu_worker, [j for j in jobs if j])
+        wall = time.perf_counter() - t0
+    V = sum(r[0] for r in res)
+    busy = max(r[1] for r in res)
+    return {"value": V / busy, "unit": "ray-cell updates/s", "cores": cores, "kind": "port",
+            "sample": f"tick 0 of all {len(specs)} maps, maps spread over {cores} processes "
+                      f"(slowest process {busy:.1f} s, {wall:.1f} s with start-up); one core: "
+                      f"{V / sum(r[1] for r in res):.4g} ray-cell updates/s"}
+
+
 def run_multimap(args):
     import torch
     import bonxai_gb300 as bx
@@ -685,6 +722,9 @@ def run_multimap(args):
     t_b, t_p, dev_b, V_b, V_p = 0.0, 0.0, 0.0, 0, 0
     lat = []
     phases = {}
+    launches0 = batch.stats()["launches"]
+    clk = ClockSampler(dev.index)
+    clk.__enter__()
     for t in range(ticks):
         scans = multimap_tick(specs, base, t)
         pts = torch.from_numpy(np.concatenate([s[0] for s in scans])).to(dev)
@@ -719,10 +759,37 @@ def run_multimap(args):
             V_p += vp
         if rc.sum() != vp:
             raise SystemExit(f"tick {t}: batched {int(rc.sum())} != plain {vp} ray cells")
+    clk.__exit__(None, None, None)
+    launches = batch.stats()["launches"] - launches0
     # bit-exact check of every map after the run
     same = all(np.array_equal(bmaps[i].dump()[1], pmaps[i].dump()[1]) for i in range(n_maps))
     value = V_b / t_b
     plain = V_p / t_p
+    # e2e: the same ticks from pinned host memory through the C ABI (the batch
+    # copies the points to the device inside the call)
+    e2e = None
+    if not args.no_e2e:
+        emaps = [bx.ProbabilisticMap(sp.resolution, big) for sp in specs]
+        t_e, V_e = 0.0, 0
+        for t in range(ticks):
+            scans = multimap_tick(specs, base, t)
+            hp = torch.from_numpy(np.concatenate([s[0] for s in scans])).pin_memory().numpy()
+            off = np.concatenate([[0], np.cumsum([len(s[0]) for s in scans])]).astype(np.uint64)
+            org = np.stack([s[1] for s in scans])
+            torch.cuda.synchronize()
+            a = time.perf_counter()
+            rc = batch.insert(emaps, hp, off, org, MM_RANGE)
+            dt = time.perf_counter() - a
+            if t >= args.warmup:
+                t_e += dt
+                V_e += int(rc.sum())
+        e2e = {"value": V_e / t_e, "unit": "ray-cell updates/s",
+               "h2d_bytes_per_step": int(off[-1]) * 12, "d2h_bytes_per_step": n_maps * 8}
+        for m in emaps:
+            m.close()
+    cpu = None
+    if not args.no_cpu:
+        cpu = mm_cpu_baseline(specs, multimap_tick(specs, base, 0), os.cpu_count() or 1)
     lat.sort()
     line = {
         "metric": "ray-cell updates/s (64-map batched tick)", "value": value,
@@ -740,6 +807,7 @@ def run_multimap(args):
         "tick_ms_p50": lat[len(lat) // 2], "tick_ms_p99": lat[min(len(lat) - 1, int(0.99 * len(lat)))],
         "maps_bit_identical_batched_vs_plain": same,
         "tick_phase_ms": phases,
+        "e2e": e2e, "cpu_baseline": cpu, "gpu_launches": launches, "clocks": clk.summary(),
     }
     print(json.dumps(line), flush=True)
     return 0
@@ -858,7 +926,7 @@ def main():
     ap.add_argument("--duration", type=float, default=20.0, help="seconds of load (serve)")
     ap.add_argument("--budget-gb", type=int, default=40)
     ap.add_argument("--rays-per-warp", type=int, default=1)
-    ap.add_argument("--ray-unroll", type=int, default=2)
+    ap.add_argument("--ray-unroll", type=int, default=1)
     ap.add_argument("--block-size", type=int, default=0)
     ap.add_argument("--flags", type=int, default=0, help="extra BXG_FLAG_* bits for the maps")
     ap.add_argument("--cpu-seconds", type=float, default=10.0,

@@ -129,7 +129,7 @@ MapCore::~MapCore() {
   if (device >= 0) cudaSetDevice(device);
   if (stream) cudaStreamSynchronize(stream);
   for (DevBuf* b : {&buckets, &ichild, &imask, &lmask, &ldata, &lkey, &lfree, &ctr, &s_in,
-                    &s_in2, &s_out, &s_out2, &s_dedup, &s_dedup2, &s_ep, &s_cast, &s_tmp})
+                    &s_in2, &s_out, &s_out2, &s_dedup, &s_dedup2, &s_ep, &s_cast, &s_tmp, &s_dir})
     b->release();
   if (h_ctr) cudaFreeHost(h_ctr);
   if (own_stream && stream) cudaStreamDestroy(stream);

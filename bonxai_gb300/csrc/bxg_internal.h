@@ -85,6 +85,7 @@ struct MapCore {
   // the table the last endpoint phase used, so the next one needs no memset)
   uint32_t dedup_clean = 0;
   uint32_t dedup_used = 0;  // entries the last endpoint phase used
+  DevBuf s_dir;             // leaf directory of the ray kernel (bxg_scan.cuh)
 
   std::string err;
   uint64_t launches = 0;
@@ -160,6 +161,8 @@ struct bxg_pmap_s {
   uint64_t last_stats[8] = {0};
   float last_times[4] = {0};
   uint32_t last_new_leaves = 0;  // leaves created by the last scan (pool headroom)
+  double dir_reach = 0;          // cells of the coming ray phase lie within this range
+  uint32_t dir_epoch = 0;        // leaf-directory epoch of the last scan (1..15)
   cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   ~bxg_pmap_s() {
     for (auto& e : ev)
@@ -168,6 +171,11 @@ struct bxg_pmap_s {
 };
 
 namespace bxg {
+struct LeafDir;
+// Sets up the ray walk's leaf directory of a scan (bxg_pmap.cu).
+// Memsets (first use, epoch wrap) go to `stream` (nullptr: the map's own).
+int leaf_dir_for_scan(bxg_pmap_s* pm, int ox, int oy, int oz, LeafDir* D, size_t max_words,
+                      cudaStream_t stream);
 // Completes a scan whose endpoints were listed (and possibly applied) by a
 // batched tick but whose map ran out of pool: grows the pools and re-runs the
 // idempotent endpoint completion and ray phases on the map's own stream.

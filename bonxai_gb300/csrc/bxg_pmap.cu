@@ -202,7 +202,8 @@ template <int W, int U>
 __global__ void __launch_bounds__(256, U == 2 ? 3 : 4) k_rays(DMap M, const int4* __restrict__ cast,
                                                  uint32_t cast_cap, int ox, int oy, int oz,
                                                  int32_t u, int32_t miss, int32_t cmin,
-                                                 uint4* __restrict__ tab, uint32_t tab_n) {
+                                                 uint4* __restrict__ tab, uint32_t tab_n,
+                                                 LeafDir D) {
   for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < tab_n; t += gridDim.x * blockDim.x)
     tab[t] = make_uint4(kNone, kNone, kNone, kNone);
   const uint32_t n_cast = min(ld_volatile(M.ctr + C_CAST), cast_cap);
@@ -217,7 +218,8 @@ __global__ void __launch_bounds__(256, U == 2 ? 3 : 4) k_rays(DMap M, const int4
     if (U == 2)
       walk_ray2<W>(M, cast[r], ox, oy, oz, u, miss, cmin, sl, gbase, gmask, visited, updated);
     else
-      walk_ray<W>(M, cast[r], ox, oy, oz, u, miss, cmin, sl, gbase, gmask, visited, updated);
+      walk_ray<W, true>(M, cast[r], ox, oy, oz, u, miss, cmin, sl, gbase, gmask, visited,
+                        updated, D.words ? &D : nullptr);
   }
   visited = __reduce_add_sync(0xffffffffu, visited);
   updated = __reduce_add_sync(0xffffffffu, updated);
@@ -357,6 +359,46 @@ int launch_apply(bxg_pmap_s* pm) {
   return BXG_OK;
 }
 
+}  // namespace
+
+namespace bxg {
+// The leaf directory for a scan from (ox, oy, oz) whose ray cells lie within
+// pm->dir_reach of the origin: a cube of leaves covering every such cell, when
+// it has at most max_words words and leaf slots fit in 28 bits. Otherwise *D
+// stays empty (the walk then probes the root hash for every leaf run).
+int leaf_dir_for_scan(bxg_pmap_s* pm, int ox, int oy, int oz, LeafDir* D, size_t max_words,
+                      cudaStream_t stream) {
+  MapCore* m = &pm->core;
+  if (!stream) stream = m->stream;
+  *D = LeafDir{};
+  if (!(pm->dir_reach > 0) || m->dm.lcap >= (1u << 28)) return BXG_OK;
+  const double cells = std::ceil(pm->dir_reach * m->inv_res) + 2;
+  const double half = std::ceil(cells / double(1 << m->dm.lb)) + 1;
+  if (!(half < 128)) return BXG_OK;
+  const uint32_t side = uint32_t(2 * half + 1);
+  const size_t words = size_t(side) * side * side;
+  if (words > max_words) return BXG_OK;
+  if (m->s_dir.cap < words * 4) {
+    BXG_CUDA(m, m->s_dir.ensure(words * 4));
+    BXG_CUDA(m, cudaMemsetAsync(m->s_dir.p, 0, m->s_dir.cap, stream));
+    pm->dir_epoch = 0;
+  }
+  if (++pm->dir_epoch == 16) {  // the epoch wraps: clear once every 15 scans
+    BXG_CUDA(m, cudaMemsetAsync(m->s_dir.p, 0, words * 4, stream));
+    pm->dir_epoch = 1;
+  }
+  D->words = m->s_dir.as<uint32_t>();
+  D->side = side;
+  D->x0 = (ox >> m->dm.lb) - int(half);
+  D->y0 = (oy >> m->dm.lb) - int(half);
+  D->z0 = (oz >> m->dm.lb) - int(half);
+  D->epoch = pm->dir_epoch;
+  return BXG_OK;
+}
+}  // namespace bxg
+
+namespace {
+
 int launch_rays(bxg_pmap_s* pm, int ox, int oy, int oz) {
   MapCore* m = &pm->core;
   const uint32_t rpw = m->rays_per_warp ? m->rays_per_warp : 1;
@@ -374,15 +416,18 @@ int launch_rays(bxg_pmap_s* pm, int ox, int oy, int oz) {
   const int32_t uc = pm->update_count;
   uint4* const tab = m->s_dedup.as<uint4>();
   const uint32_t tab_n = m->dedup_used;
+  LeafDir dir{};
+  int st = leaf_dir_for_scan(pm, ox, oy, oz, &dir, size_t(1) << 24, m->stream);
+  if (st) return st;
   if (rpw == 4) {
-    if (u2) k_rays<8, 2><<<g, b, 0, m->stream>>>(m->dm, c, ccap, ox, oy, oz, uc, o.miss, o.cmin, tab, tab_n);
-    else k_rays<8, 1><<<g, b, 0, m->stream>>>(m->dm, c, ccap, ox, oy, oz, uc, o.miss, o.cmin, tab, tab_n);
+    if (u2) k_rays<8, 2><<<g, b, 0, m->stream>>>(m->dm, c, ccap, ox, oy, oz, uc, o.miss, o.cmin, tab, tab_n, dir);
+    else k_rays<8, 1><<<g, b, 0, m->stream>>>(m->dm, c, ccap, ox, oy, oz, uc, o.miss, o.cmin, tab, tab_n, dir);
   } else if (rpw == 2) {
-    if (u2) k_rays<16, 2><<<g, b, 0, m->stream>>>(m->dm, c, ccap, ox, oy, oz, uc, o.miss, o.cmin, tab, tab_n);
-    else k_rays<16, 1><<<g, b, 0, m->stream>>>(m->dm, c, ccap, ox, oy, oz, uc, o.miss, o.cmin, tab, tab_n);
+    if (u2) k_rays<16, 2><<<g, b, 0, m->stream>>>(m->dm, c, ccap, ox, oy, oz, uc, o.miss, o.cmin, tab, tab_n, dir);
+    else k_rays<16, 1><<<g, b, 0, m->stream>>>(m->dm, c, ccap, ox, oy, oz, uc, o.miss, o.cmin, tab, tab_n, dir);
   } else {
-    if (u2) k_rays<32, 2><<<g, b, 0, m->stream>>>(m->dm, c, ccap, ox, oy, oz, uc, o.miss, o.cmin, tab, tab_n);
-    else k_rays<32, 1><<<g, b, 0, m->stream>>>(m->dm, c, ccap, ox, oy, oz, uc, o.miss, o.cmin, tab, tab_n);
+    if (u2) k_rays<32, 2><<<g, b, 0, m->stream>>>(m->dm, c, ccap, ox, oy, oz, uc, o.miss, o.cmin, tab, tab_n, dir);
+    else k_rays<32, 1><<<g, b, 0, m->stream>>>(m->dm, c, ccap, ox, oy, oz, uc, o.miss, o.cmin, tab, tab_n, dir);
   }
   BXG_LAUNCHED(m);
   m->dedup_clean = std::max(m->dedup_clean, tab_n);
@@ -444,6 +489,27 @@ int finish_scan(bxg_pmap_s* pm, int ox, int oy, int oz, bool cast_rays, uint64_t
   return core_maintain(m);
 }
 
+// Σ Chebyshev length from origin cell o of the rays queued by addHitPoint /
+// addMissPoint batches (their add-time lengths were measured from (0,0,0)):
+// read back and summed on the host; this path is not the streaming one.
+int queued_ray_cells(bxg_pmap_s* pm, const int* o, uint64_t* len) {
+  MapCore* m = &pm->core;
+  *len = 0;
+  if (!pm->cast_ub) return BXG_OK;
+  int st = core_sync(m);
+  if (st) return st;
+  const uint32_t n_cast = m->h_ctr[C_CAST];
+  if (!n_cast) return BXG_OK;
+  std::vector<int4> h(n_cast);
+  BXG_CUDA(m, cudaMemcpy(h.data(), m->s_cast.p, size_t(n_cast) * 16, cudaMemcpyDeviceToHost));
+  for (const int4& e : h) {
+    const int64_t dx = std::llabs(int64_t(e.x) - o[0]), dy = std::llabs(int64_t(e.y) - o[1]),
+                  dz = std::llabs(int64_t(e.z) - o[2]);
+    *len += uint64_t(std::max(dx, std::max(dy, dz)));
+  }
+  return BXG_OK;
+}
+
 int origin_coord(const MapCore* m, double x, double y, double z, int* c) {
   c[0] = static_cast<int>(std::floor(x * m->inv_res));
   c[1] = static_cast<int>(std::floor(y * m->inv_res));
@@ -466,6 +532,13 @@ int insert_impl(bxg_pmap m_, const PT* xyz, size_t stride, size_t n, const PT* o
                fz = static_cast<double>(origin[2]);
   int o[3];
   origin_coord(m, fx, fy, fz, o);
+  // rays queued by earlier addHitPoint/addMissPoint batches are cast by this
+  // scan too (updateFreeCells, probabilistic_map.hpp:159): count their cells
+  uint64_t queued = 0;
+  if (ray_cells && pm->cast_ub) {
+    const int qs = queued_ray_cells(pm, o, &queued);
+    if (qs) return qs;
+  }
   // Headroom for this scan's new leaves (twice the last scan's, at least a
   // quarter of the points), so that the scan rarely has to grow and re-run.
   const uint32_t leaves_before = m->h_ctr[C_LEAF];
@@ -483,6 +556,9 @@ int insert_impl(bxg_pmap m_, const PT* xyz, size_t stride, size_t n, const PT* o
     if (st) return st;
     const double mr2 = max_range * max_range;
     const int keep = (m->flags & BXG_FLAG_KEEP_NONFINITE) ? 1 : 0;
+    // rays of this scan end within max_range of the origin (hits are closer);
+    // rays queued by earlier add batches may not: no directory then
+    pm->dir_reach = pm->cast_ub == 0 ? max_range : 0.0;
     const int zero = ZERO_STATS | (pm->cast_ub == 0 ? ZERO_CAST : 0);
     EpFast fast = make_ep_fast(fx, fy, fz, max_range, m->inv_res);
     if (sizeof(PT) != 4) fast.on = 0;
@@ -511,8 +587,10 @@ int insert_impl(bxg_pmap m_, const PT* xyz, size_t stride, size_t n, const PT* o
     return BXG_OK;
   }
   st = finish_scan(pm, o[0], o[1], o[2], true, ray_cells, true);
-  if (!st)
+  if (!st) {
     pm->last_new_leaves = m->h_ctr[C_LEAF] > leaves_before ? m->h_ctr[C_LEAF] - leaves_before : 0;
+    if (ray_cells) *ray_cells += queued;
+  }
   return st;
 }
 
@@ -681,7 +759,8 @@ int pmap_complete_scan(bxg_pmap_s* pm, const int4* d_cast, const uint32_t* d_cou
     BXG_LAUNCHED(m);
     const unsigned rblocks = unsigned(std::min<uint64_t>((cap + 7) / 8, uint64_t(m->sm_count) * 8));
     k_rays<32, 1><<<std::max(rblocks, 1u), 256, 0, m->stream>>>(m->dm, d_cast, cap, ox, oy, oz,
-                                                               u, o.miss, o.cmin, nullptr, 0);
+                                                               u, o.miss, o.cmin, nullptr, 0,
+                                                               LeafDir{});
     BXG_LAUNCHED(m);
     st = core_sync(m, &err);
     if (st && !(err & (ERR_POOL_INNER | ERR_POOL_LEAF | ERR_HASH_FULL))) return st;
@@ -801,22 +880,10 @@ int bxg_pmap_update_free_cells(bxg_pmap pm, const double origin[3], uint64_t* ra
   cudaSetDevice(m->device);
   int o[3];
   origin_coord(m, origin[0], origin[1], origin[2], o);
-  // the ray lengths counted at add time were measured from (0,0,0); recount
-  // them for this origin on the host-visible path
-  if (ray_cells) {
-    int st = core_sync(m);
-    if (st) return st;
-  }
-  const uint32_t n_cast = pm->cast_ub ? m->h_ctr[C_CAST] : 0;  // the device count is stale
   uint64_t len = 0;
-  if (ray_cells && n_cast) {
-    std::vector<int4> h(n_cast);
-    BXG_CUDA(m, cudaMemcpy(h.data(), m->s_cast.p, size_t(n_cast) * 16, cudaMemcpyDeviceToHost));
-    for (const int4& e : h) {
-      const int64_t dx = std::llabs(int64_t(e.x) - o[0]), dy = std::llabs(int64_t(e.y) - o[1]),
-                    dz = std::llabs(int64_t(e.z) - o[2]);
-      len += uint64_t(std::max(dx, std::max(dy, dz)));
-    }
+  if (ray_cells) {
+    const int st = queued_ray_cells(pm, o, &len);
+    if (st) return st;
   }
   const int st = finish_scan(pm, o[0], o[1], o[2], true, nullptr, false);
   if (st) return st;

@@ -256,10 +256,25 @@ __device__ __forceinline__ bool winner_apply(const DMap& M, int4 e, int32_t u, c
 // op(act, leaf, ci, k): act = the lane has a cell (k < m), leaf = its leaf
 // slot (kNone if the pool ran out), ci = its index in the leaf, k = its
 // position on the ray.
-template <int W, class Op>
+// Leaf directory of one scan: a dense cube of `side`^3 words over the leaves
+// within max_range of the origin (x0/y0/z0: leaf coordinate of its corner).
+// A word holds (epoch << 28) | leaf slot; a word of another epoch is empty, so
+// the cube is cleared only when the 4-bit epoch wraps. A head inside the cube
+// reads one word instead of probing the root hash and the inner node, and
+// writes the slot it resolved otherwise (racing writers store the same word).
+struct LeafDir {
+  uint32_t* words;  // nullptr: no directory
+  int x0, y0, z0;
+  uint32_t side;
+  uint32_t epoch;  // 1..15, in bits 28-31 of a valid word
+};
+
+// DIR: the walk reads the leaf directory D (compiled out otherwise: the code
+// costs registers in kernels that never have one).
+template <int W, bool DIR, class Op>
 __device__ __forceinline__ void walk_ray_op(const DMap& M, int4 e, int ox, int oy, int oz,
                                             unsigned sl, unsigned gbase, unsigned gmask,
-                                            Op&& op) {
+                                            Op&& op, const LeafDir* D) {
   const int dx = e.x - ox, dy = e.y - oy, dz = e.z - oz;
   const uint32_t ax = static_cast<uint32_t>(abs(dx)), ay = static_cast<uint32_t>(abs(dy)),
                  az = static_cast<uint32_t>(abs(dz));
@@ -294,16 +309,30 @@ __device__ __forceinline__ void walk_ray_op(const DMap& M, int4 e, int ox, int o
     const bool head = act && key != q;
     uint32_t leaf = kNone;
     if (head) {
-      const int rx = cx & rm, ry = cy & rm, rz = cz & rm;
-      uint32_t in = root_probe_fast(M, rx, ry, rz);
-      if (in == kPending) in = root_get_or_create(M, rx, ry, rz);
-      if (in != kNone) {
-        const uint32_t ii = inner_index(M, cx, cy, cz);
-        leaf = M.ichild[static_cast<size_t>(in) * M.isize + ii];
-        if (leaf >= kPending) {
-          const int32_t lm = leaf_mask(M);
-          leaf = leaf_get_or_create(M, in, ii, cx & lm, cy & lm, cz & lm);
+      uint32_t* dw = nullptr;
+      if (DIR && D) {
+        const uint32_t qx = static_cast<uint32_t>((cx >> lb) - D->x0),
+                       qy = static_cast<uint32_t>((cy >> lb) - D->y0),
+                       qz = static_cast<uint32_t>((cz >> lb) - D->z0);
+        if (qx < D->side && qy < D->side && qz < D->side) {
+          dw = D->words + (static_cast<size_t>(qx) * D->side + qy) * D->side + qz;
+          const uint32_t w = *dw;
+          if ((w >> 28) == D->epoch) leaf = w & 0x0FFFFFFFu;
         }
+      }
+      if (leaf == kNone) {
+        const int rx = cx & rm, ry = cy & rm, rz = cz & rm;
+        uint32_t in = root_probe_fast(M, rx, ry, rz);
+        if (in == kPending) in = root_get_or_create(M, rx, ry, rz);
+        if (in != kNone) {
+          const uint32_t ii = inner_index(M, cx, cy, cz);
+          leaf = M.ichild[static_cast<size_t>(in) * M.isize + ii];
+          if (leaf >= kPending) {
+            const int32_t lm = leaf_mask(M);
+            leaf = leaf_get_or_create(M, in, ii, cx & lm, cy & lm, cz & lm);
+          }
+        }
+        if (DIR && dw && leaf != kNone) *dw = (D->epoch << 28) | leaf;
       }
     }
     const unsigned hm = (__ballot_sync(gmask, head) & gmask) >> gbase;
@@ -322,13 +351,13 @@ __device__ __forceinline__ void walk_ray_op(const DMap& M, int4 e, int ox, int o
 }
 
 // The ray walk with the miss update applied in place (the single-pass form).
-template <int W>
+template <int W, bool DIR = false>
 __device__ __forceinline__ void walk_ray(const DMap& M, int4 e, int ox, int oy, int oz,
                                          int32_t u, int32_t miss, int32_t cmin, unsigned sl,
                                          unsigned gbase, unsigned gmask, uint32_t& visited,
-                                         uint32_t& updated) {
+                                         uint32_t& updated, const LeafDir* D = nullptr) {
   int32_t* const cells = reinterpret_cast<int32_t*>(M.ldata);
-  walk_ray_op<W>(M, e, ox, oy, oz, sl, gbase, gmask,
+  walk_ray_op<W, DIR>(M, e, ox, oy, oz, sl, gbase, gmask,
                  [&](bool act, uint32_t leaf, uint32_t ci, uint32_t) {
                    if (act && leaf != kNone) {
                      int32_t* cp = cells + static_cast<size_t>(leaf) * M.lsize + ci;
@@ -340,7 +369,8 @@ __device__ __forceinline__ void walk_ray(const DMap& M, int4 e, int ox, int oy, 
                      }
                      visited++;
                    }
-                 });
+                 },
+                 D);
 }
 
 // Leaf slot of a head cell: the inline hash probe, else the bounded-wait

@@ -102,6 +102,48 @@ def test_scans_interleaved_with_grid_writes_and_added_points(gpu, port):
     assert_same_map(m, o)
 
 
+def test_leaf_directory_vs_oracle(gpu, port):
+    """The leaf directory of the ray walk gives the oracle's maps: 20 LiDAR scans
+    (the 4-bit epoch wraps), a clear in between, tiny pools that grow
+    mid-scan, depth frames at 0.02 m, and scans after queued hit/miss points."""
+    F = 0
+    scene = synth.LidarScene()
+    m = gpu.ProbabilisticMap(scene.resolution, gpu.Config(flags=F))
+    o = port.pmap(scene.resolution)
+    for k in range(20):
+        pts, org = scene.scan(k, n_points=8192)
+        assert m.insert_point_cloud(pts, org, scene.max_range) == o.insert(pts, org, scene.max_range)
+        if k == 9:
+            # grid().clear() keeps the scan counter (as in the reference): a
+            # fresh oracle map is advanced to the same counter by empty
+            # updateFreeCells calls
+            assert_same_map(m, o)
+            m.clear()
+            o = port.pmap(scene.resolution)
+            while o.update_count != m.update_count:
+                o.update_free_cells(np.zeros(3))
+    assert_same_map(m, o)
+    tiny = gpu.Config(flags=F, initial_leaves=16, initial_inners=4, hash_buckets=16)
+    m2 = gpu.ProbabilisticMap(scene.resolution, tiny)
+    o2 = port.pmap(scene.resolution)
+    for k in range(3):
+        pts, org = scene.scan(k, n_points=20000)
+        assert m2.insert_point_cloud(pts, org, 30.0) == o2.insert(pts, org, 30.0)
+        h = (org + np.random.default_rng(k).normal(0, 40, (200, 3))).astype(np.float64)
+        m2.add_hit_points(h)
+        o2.add_hit(h)
+    pts, org = scene.scan(5, n_points=20000)
+    assert m2.insert_point_cloud(pts, org, 30.0) == o2.insert(pts, org, 30.0)
+    assert_same_map(m2, o2)
+    room = synth.DepthRoom()
+    m3 = gpu.ProbabilisticMap(room.resolution, gpu.Config(flags=F))
+    o3 = port.pmap(room.resolution)
+    for k in range(3):
+        pts, org = room.frame(k, subsample=8)
+        assert m3.insert_point_cloud(pts, org, room.max_range) == o3.insert(pts, org, room.max_range)
+    assert_same_map(m3, o3)
+
+
 def test_depth_frames_vs_oracle(gpu, port):
     room = synth.DepthRoom()
     m = gpu.ProbabilisticMap(room.resolution)
