@@ -708,16 +708,30 @@ def mm_cpu_baseline(specs, scans, cores):
 
 
 def run_multimap(args):
+    """Under torchrun each rank takes whole maps (longest-processing-time
+    assignment by points, bonxai_gb300.sharding); no collective touches the
+    data, and rank 0 reports units summed over ranks over the slowest rank's
+    time."""
     import torch
     import bonxai_gb300 as bx
+    from bonxai_gb300 import sharding
 
-    torch.cuda.set_device(0)
-    dev = torch.device("cuda", 0)
-    n_maps = args.maps
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    dev = torch.device("cuda", torch.cuda.current_device())
     t0 = time.perf_counter()
-    specs, base = multimap_inputs(n_maps)
-    log(f"generated {n_maps} base scans in {time.perf_counter() - t0:.1f} s, "
-        f"{sum(len(b[0]) for b in base)} points per tick")
+    specs, base = multimap_inputs(args.maps)
+    mine = sharding.my_maps([len(b[0]) for b in base], ws, rank)
+    specs = [specs[i] for i in mine]
+    base = [base[i] for i in mine]
+    n_maps = len(specs)
+    log(f"rank {rank}: generated {args.maps} base scans in {time.perf_counter() - t0:.1f} s, "
+        f"{sum(len(b[0]) for b in base)} of its points per tick")
     ticks = args.warmup + args.steps
     big = bx.Config(initial_leaves=1 << 16, initial_inners=1 << 12, hash_buckets=1 << 14)
     bmaps = [bx.ProbabilisticMap(sp.resolution, big) for sp in specs]
@@ -769,6 +783,13 @@ def run_multimap(args):
     launches = batch.stats()["launches"] - launches0
     # bit-exact check of every map after the run
     same = all(np.array_equal(bmaps[i].dump()[1], pmaps[i].dump()[1]) for i in range(n_maps))
+    if ws > 1:
+        import torch.distributed as dist
+        V_b, t_b = sharding.aggregate(V_b, t_b)
+        V_p, t_p = sharding.aggregate(V_p, t_p)
+        ok = torch.tensor([1.0 if same else 0.0], device=dev)
+        dist.all_reduce(ok, op=dist.ReduceOp.MIN)
+        same = bool(ok.item())
     value = V_b / t_b
     plain = V_p / t_p
     # e2e: the same ticks from pinned host memory through the C ABI (the batch
@@ -789,21 +810,28 @@ def run_multimap(args):
             if t >= args.warmup:
                 t_e += dt
                 V_e += int(rc.sum())
+        h2d = int(off[-1]) * 12
+        if ws > 1:
+            V_e, t_e = sharding.aggregate(V_e, t_e)
         e2e = {"value": V_e / t_e, "unit": "ray-cell updates/s",
-               "h2d_bytes_per_step": int(off[-1]) * 12, "d2h_bytes_per_step": n_maps * 8}
+               "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": n_maps * 8}
         for m in emaps:
             m.close()
+    if rank != 0:
+        dist.destroy_process_group()
+        return 0
     cpu = None
-    if not args.no_cpu:
+    if not args.no_cpu and ws == 1:
         cpu = mm_cpu_baseline(specs, multimap_tick(specs, base, 0), os.cpu_count() or 1)
     lat.sort()
     line = {
         "metric": "ray-cell updates/s (64-map batched tick)", "value": value,
-        "unit": "ray-cell updates/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "unit": "ray-cell updates/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * t_b / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "int32", "data": "synthetic",
-        "config": {"workload": "multimap_64", "maps": n_maps,
-                   "points_per_tick": int(off[-1]), "max_range_m": MM_RANGE,
+        "config": {"workload": "multimap_64", "maps": args.maps,
+                   "parallelism": f"maps sharded over {ws} rank(s)",
+                   "points_per_tick_rank0": int(off[-1]), "max_range_m": MM_RANGE,
                    "resolutions_m": [0.02, 0.05, 0.1], "sizes": "log-uniform 10k..500k",
                    "rays_per_warp": args.rays_per_warp, "ray_unroll": args.ray_unroll,
                    "graph": batch.stats()["graph"],
@@ -816,6 +844,8 @@ def run_multimap(args):
         "e2e": e2e, "cpu_baseline": cpu, "gpu_launches": launches, "clocks": clk.summary(),
     }
     print(json.dumps(line), flush=True)
+    if ws > 1:
+        dist.destroy_process_group()
     return 0
 
 
