@@ -240,11 +240,13 @@ __global__ void k_query(DMap M, const int32_t* __restrict__ xyz, uint32_t n, int
   bool have = false;
   int32_t p = 0;
   if (lf != kNone) {
+    // The cell word first: an on cell of a ProbabilisticMap has update_id in
+    // 1..3 (a nonzero word), an off cell holds zero, so only a zero word
+    // needs the mask bit (it may be an on cell written through the grid).
     const uint32_t ci = leaf_index(M, x, y, z);
-    if (cell_is_on(M, lf, ci)) {
-      have = true;
-      p = cell_prob(reinterpret_cast<const int32_t*>(M.ldata)[size_t(lf) * M.lsize + ci]);
-    }
+    const int32_t w = reinterpret_cast<const int32_t*>(M.ldata)[size_t(lf) * M.lsize + ci];
+    have = w != 0 || cell_is_on(M, lf, ci);
+    p = cell_prob(w);
   }
   uint8_t r;
   if (mode == 0)

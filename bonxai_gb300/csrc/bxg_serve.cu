@@ -59,12 +59,11 @@ __global__ void k_query_multi(const QueryDesc* __restrict__ d, uint32_t nd,
     const uint32_t lf = leaf_of(q.M, x, y, z, false);
     bool have = false;
     int32_t p = 0;
-    if (lf != kNone) {
+    if (lf != kNone) {  // cell word first; the mask only for a zero word (as k_query)
       const uint32_t ci = leaf_index(q.M, x, y, z);
-      if (cell_is_on(q.M, lf, ci)) {
-        have = true;
-        p = cell_prob(reinterpret_cast<const int32_t*>(q.M.ldata)[size_t(lf) * q.M.lsize + ci]);
-      }
+      const int32_t w = reinterpret_cast<const int32_t*>(q.M.ldata)[size_t(lf) * q.M.lsize + ci];
+      have = w != 0 || cell_is_on(q.M, lf, ci);
+      p = cell_prob(w);
     }
     out[i] = q.mode == 0 ? (have && p > q.thr) : q.mode == 1 ? (have ? p == q.thr : 1)
                                                                 : (have && p < q.thr);

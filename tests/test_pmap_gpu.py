@@ -343,3 +343,36 @@ def test_endpoint_filter_adversarial(gpu, port, res, origin, max_range):
     bx_, bc = bm.dump()
     ox, oc = o.dump()
     assert np.array_equal(bx_, ox) and np.array_equal(bc, oc)
+
+
+def test_queries_on_cells_with_zero_words(gpu):
+    """isOccupied/isUnknown/isFree read the cell word first and the mask only
+    for a zero word: cells turned on with a zero word through the grid view
+    (and a negative threshold, so that 0 counts as occupied) still answer as
+    probabilistic_map.cpp:56-75 does for an existing cell."""
+    scene = synth.LidarScene()
+    m = gpu.ProbabilisticMap(0.1)
+    pts, org = scene.scan(0, n_points=20000)
+    m.insert_point_cloud(pts, org, 30.0)
+    lib = gpu.load_library()
+    xyz, cells = m.dump()
+    zero_on = np.ascontiguousarray(xyz[::5])
+    fresh = np.ascontiguousarray(np.array([[9000 + k, -9000, 5] for k in range(50)], np.int32))
+    both = np.ascontiguousarray(np.concatenate([zero_on, fresh]))
+    zeros = np.zeros(len(both), np.int32)
+    assert lib.bxg_grid_set_values(lib.bxg_pmap_grid(m.h), both.ctypes.data, zeros.ctypes.data,
+                                   len(both), None) == 0
+    opts = m.options
+    opts[4] = -5
+    m.options = opts
+    xyz, cells = m.dump()
+    on = {tuple(c): int(w) >> 4 for c, w in zip(xyz, cells)}
+    q = np.concatenate([xyz[::3], fresh, fresh + 1, synth.lookup_coords(xyz.min(0), xyz.max(0),
+                                                                          20000, seed=9)])
+    q = np.ascontiguousarray(q.astype(np.int32))
+    want_occ = np.array([tuple(c) in on and on[tuple(c)] > -5 for c in q], np.uint8)
+    want_unk = np.array([tuple(c) not in on or on[tuple(c)] == -5 for c in q], np.uint8)
+    want_fre = np.array([tuple(c) in on and on[tuple(c)] < -5 for c in q], np.uint8)
+    assert np.array_equal(m.is_occupied(q), want_occ)
+    assert np.array_equal(m.is_unknown(q), want_unk)
+    assert np.array_equal(m.is_free(q), want_fre)
