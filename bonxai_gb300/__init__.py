@@ -119,6 +119,7 @@ _SIGS = {
     "bxg_pmap_kernel_times": (_int, [_vp, _vp]),
     "bxg_pmap_stream": (_vp, [_vp]),
     "bxg_pmap_grid": (_vp, [_vp]),
+    "bxg_debug_hold_leaf": (_int, [_vp, _vp]),
     "bxg_pmap_add_points": (_int, [_vp, _vp, _vp, _sz]),
     "bxg_grid_store_if_on": (_int, [_vp, _vp, _vp, _sz]),
     "bxg_compute_rays": (_int, [_vp, _vp, _sz, _vp, _vp, _vp]),

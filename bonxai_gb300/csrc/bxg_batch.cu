@@ -639,9 +639,9 @@ int bxg_batch_insert_f32(bxg_batch b, const bxg_pmap* maps, size_t n_scans, cons
         b->err = m->err;
       }
     } else if (e) {
-      core_sync(m);  // clears the bits and records the message
+      const int cs = core_sync(m);  // clears the bits, maps them to a status
       if (!status) {
-        status = BXG_ERR_INVALID_ARG;
+        status = cs ? cs : BXG_ERR_INVALID_ARG;
         b->err = m->err;
       }
     }

@@ -372,14 +372,15 @@ int core_sync(MapCore* m, uint32_t* err_bits_out) {
     BXG_CUDA(m, cudaStreamSynchronize(m->stream));
   }
   if (!err) return BXG_OK;
-  if (err & (ERR_POOL_INNER | ERR_POOL_LEAF))
-    return set_error(m, BXG_ERR_OUT_OF_POOL, "node pool exhausted");
-  if (err & ERR_HASH_FULL) return set_error(m, BXG_ERR_HASH_FULL, "root hash full");
+  // errors that growing the pools cannot cure come first
   if (err & ERR_WAIT)
     return set_error(m, BXG_ERR_WAIT_TIMEOUT, "a bounded device-side wait gave up");
   if (err & ERR_RAY_TOO_LONG)
     return set_error(m, BXG_ERR_INVALID_ARG, "a ray is longer than 2^26 cells");
   if (err & ERR_SCRATCH) return set_error(m, BXG_ERR_INVALID_ARG, "scratch table overflow");
+  if (err & (ERR_POOL_INNER | ERR_POOL_LEAF))
+    return set_error(m, BXG_ERR_OUT_OF_POOL, "node pool exhausted");
+  if (err & ERR_HASH_FULL) return set_error(m, BXG_ERR_HASH_FULL, "root hash full");
   return set_error(m, BXG_ERR_CUDA, "unknown device error");
 }
 

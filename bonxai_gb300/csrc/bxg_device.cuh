@@ -254,6 +254,7 @@ static __device__ __noinline__ uint32_t root_value_wait(const DMap& M, uint4* b)
       }
       continue;
     }
+    if (ld_volatile(M.ctr + C_ERR) & ERR_WAIT) return kNone;
     __nanosleep(ns);
     ns = ns < 1024 ? ns * 2 : 1024;
   }
@@ -333,6 +334,8 @@ static __device__ __noinline__ uint32_t leaf_get_or_create(const DMap& M, uint32
       c = old;
       continue;
     }
+    // another wait of this launch already gave up: the call fails anyway
+    if (ld_volatile(M.ctr + C_ERR) & ERR_WAIT) return kNone;
     __nanosleep(ns);
     ns = ns < 1024 ? ns * 2 : 1024;
     c = ld_volatile(slot);

@@ -282,6 +282,19 @@ uint32_t next_pow2(uint64_t v) {
 
 int check_grid(bxg_grid g) { return g ? BXG_OK : BXG_ERR_INVALID_ARG; }
 
+// Test hook for the bounded waits: marks the inner-node slot of the leaf
+// holding (x, y, z) as being created (kPending) by a creator that never
+// publishes, so every access to that leaf waits out its spin limit and sets
+// ERR_WAIT. *held = 1 when the slot was empty and is now held.
+__global__ void k_hold_leaf(DMap M, int x, int y, int z, int* held) {
+  *held = 0;
+  const int32_t rm = root_mask(M);
+  const uint32_t in = root_get_or_create(M, x & rm, y & rm, z & rm);
+  if (in == kNone) return;
+  uint32_t* slot = M.ichild + static_cast<size_t>(in) * M.isize + inner_index(M, x, y, z);
+  if (atomicCAS(slot, kNone, kPending) == kNone) *held = 1;
+}
+
 // Builds the dedup table for n device coordinates.
 int build_dedup(MapCore* m, const int32_t* dxyz, uint32_t n, bool keep_max, bool need_min,
                 uint32_t* tmask_out, uint32_t** tab_min_out) {
@@ -322,7 +335,9 @@ int run_with_growth(MapCore* m, F&& body) {
     uint32_t err = 0;
     st = core_sync(m, &err);
     if (st == BXG_OK) return core_maintain(m);
-    if (!(err & (ERR_POOL_INNER | ERR_POOL_LEAF | ERR_HASH_FULL))) return st;
+    if (!(err & (ERR_POOL_INNER | ERR_POOL_LEAF | ERR_HASH_FULL)) ||
+        (err & (ERR_WAIT | ERR_RAY_TOO_LONG | ERR_SCRATCH)))
+      return st;
     const int g = core_grow_for(m, err);
     if (g) return g;
   }
@@ -705,6 +720,21 @@ int bxg_grid_synchronize(bxg_grid g) {
   if (check_grid(g)) return BXG_ERR_INVALID_ARG;
   cudaSetDevice(g->core.device);
   return core_sync(&g->core);
+}
+
+int bxg_debug_hold_leaf(bxg_grid g, const int32_t xyz[3]) {
+  if (check_grid(g) || !xyz) return BXG_ERR_INVALID_ARG;
+  MapCore* m = &g->core;
+  cudaSetDevice(m->device);
+  BXG_CUDA(m, m->s_tmp.ensure(8));
+  k_hold_leaf<<<1, 1, 0, m->stream>>>(m->dm, xyz[0], xyz[1], xyz[2], m->s_tmp.as<int>());
+  BXG_LAUNCHED(m);
+  int held = 0;
+  BXG_CUDA(m, cudaMemcpyAsync(&held, m->s_tmp.p, 4, cudaMemcpyDeviceToHost, m->stream));
+  const int st = core_sync(m);
+  if (st) return st;
+  if (held != 1) return set_error(m, BXG_ERR_INVALID_ARG, "the leaf exists or cannot be reached");
+  return BXG_OK;
 }
 
 int bxg_grid_device_view(bxg_grid g, bxg_device_view* out) {

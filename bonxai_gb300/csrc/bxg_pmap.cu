@@ -462,7 +462,9 @@ int finish_scan(bxg_pmap_s* pm, int ox, int oy, int oz, bool cast_rays, uint64_t
     uint32_t err = 0;
     st = core_sync(m, &err);
     if (st == BXG_OK) break;
-    if (!(err & (ERR_POOL_INNER | ERR_POOL_LEAF | ERR_HASH_FULL))) return st;
+    if (!(err & (ERR_POOL_INNER | ERR_POOL_LEAF | ERR_HASH_FULL)) ||
+        (err & (ERR_WAIT | ERR_RAY_TOO_LONG | ERR_SCRATCH)))
+      return st;
     const int g = core_grow_for(m, err);
     if (g) return g;
   }
@@ -750,7 +752,9 @@ int pmap_complete_scan(bxg_pmap_s* pm, const int4* d_cast, const uint32_t* d_cou
   const Opts o = opts_of(pm);
   uint32_t err = 0;
   int st = core_sync(m, &err);  // reads and clears what the tick left
-  if (st && !(err & (ERR_POOL_INNER | ERR_POOL_LEAF | ERR_HASH_FULL))) return st;
+  if (st && (!(err & (ERR_POOL_INNER | ERR_POOL_LEAF | ERR_HASH_FULL)) ||
+              (err & (ERR_WAIT | ERR_RAY_TOO_LONG | ERR_SCRATCH))))
+    return st;
   BXG_CUDA(m, cudaMemcpyAsync(m->ctr.as<uint32_t>() + C_CAST, d_count, 4,
                               cudaMemcpyDeviceToDevice, m->stream));
   for (int attempt = 0; attempt < 12 && err; attempt++) {
@@ -765,7 +769,9 @@ int pmap_complete_scan(bxg_pmap_s* pm, const int4* d_cast, const uint32_t* d_cou
                                                                LeafDir{});
     BXG_LAUNCHED(m);
     st = core_sync(m, &err);
-    if (st && !(err & (ERR_POOL_INNER | ERR_POOL_LEAF | ERR_HASH_FULL))) return st;
+    if (st && (!(err & (ERR_POOL_INNER | ERR_POOL_LEAF | ERR_HASH_FULL)) ||
+              (err & (ERR_WAIT | ERR_RAY_TOO_LONG | ERR_SCRATCH))))
+    return st;
   }
   BXG_CUDA(m, cudaMemsetAsync(m->ctr.as<uint32_t>() + C_CAST, 0, 4, m->stream));
   BXG_CUDA(m, cudaStreamSynchronize(m->stream));

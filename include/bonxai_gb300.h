@@ -178,6 +178,14 @@ typedef struct {
 } bxg_device_view;
 int bxg_grid_device_view(bxg_grid g, bxg_device_view* out);
 
+/* Test hook (no counterpart in the reference): marks the leaf that would hold
+ * xyz as being created by a creator that never finishes. Any later access to
+ * that leaf waits out the device-side spin limit (about a second) and the call
+ * returns BXG_ERR_WAIT_TIMEOUT with the handle still usable; clear() releases
+ * the mark. For tests of the bounded waits only. BXG_ERR_INVALID_ARG if that
+ * leaf already exists. */
+int bxg_debug_hold_leaf(bxg_grid g, const int32_t xyz[3]);
+
 /* Serialize(out, grid) (bonxai_core/include/bonxai/serialization.hpp:77-116):
  * the reference's byte format -- header line
  * "Bonxai::VoxelGrid<type_name,inner_bits,leaf_bits>(resolution)\n", uint32
