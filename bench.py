@@ -76,7 +76,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
-                 "--format=csv,noheader,nounits", "-lms", "100"],
+                 "--format=csv,noheader,nounits", "-lms", "20"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -545,7 +545,7 @@ def run_depth(args):
     torch.cuda.set_device(local if ws > 1 else 0)
     dev = torch.device("cuda", torch.cuda.current_device())
     room = synth.DepthRoom()
-    n_frames = max(args.steps, 1) + args.warmup
+    n_frames = min(max(args.steps, 1), 20) + args.warmup  # timed frames cycle through 20
     frames = [room.frame(k) for k in range(n_frames)]
     d_frames = [(torch.from_numpy(p).to(dev), o) for p, o in frames]
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device=dev)
@@ -561,7 +561,9 @@ def run_depth(args):
         for k in range(args.steps):
             flush.fill_(k)
             torch.cuda.synchronize()
-            V += m.insert_point_cloud(*d_frames[args.warmup + k], room.max_range)
+            if k and k % 20 == 0:
+                m.clear()
+            V += m.insert_point_cloud(*d_frames[args.warmup + k % 20], room.max_range)
             t = m.kernel_times()
             ms += sum(t)
             ray_ms.append(t[3])
@@ -592,7 +594,9 @@ def run_depth(args):
     t_e2e, V_e2e = 0.0, 0
     m.clear()
     for k in range(args.steps):
-        p, o = frames[args.warmup + k]
+        if k and k % 20 == 0:
+            m.clear()
+        p, o = frames[args.warmup + k % 20]
         t0 = time.perf_counter()
         V_e2e += m.insert_point_cloud(p, o, room.max_range)
         t_e2e += time.perf_counter() - t0
@@ -601,7 +605,8 @@ def run_depth(args):
         from oracle import oracle as O
         om = O.port().pmap(room.resolution)
         t0 = time.perf_counter()
-        Vc = sum(om.insert(*frames[args.warmup + k], room.max_range) for k in range(min(3, args.steps)))
+        Vc = sum(om.insert(*frames[args.warmup + k], room.max_range)
+                 for k in range(min(3, args.steps, 20)))
         tc = time.perf_counter() - t0
         cpu = {"value": Vc / tc, "unit": "ray-cell updates/s", "cores": 1, "kind": "port",
                "sample": f"{min(3, args.steps)} frames, one thread, {tc:.2f} s"}
@@ -951,7 +956,7 @@ def run_serve(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="lidar",
