@@ -120,6 +120,7 @@ _SIGS = {
     "bxg_pmap_stream": (_vp, [_vp]),
     "bxg_pmap_grid": (_vp, [_vp]),
     "bxg_debug_hold_leaf": (_int, [_vp, _vp]),
+    "bxg_pmap_last_query_ms": (_int, [_vp, _vp]),
     "bxg_pmap_add_points": (_int, [_vp, _vp, _vp, _sz]),
     "bxg_grid_store_if_on": (_int, [_vp, _vp, _vp, _sz]),
     "bxg_compute_rays": (_int, [_vp, _vp, _sz, _vp, _vp, _vp]),
@@ -495,6 +496,12 @@ class ProbabilisticMap(_Handle):
         return self._query(self.lib.bxg_pmap_is_free, coords, out)
 
     isOccupied, isUnknown, isFree = is_occupied, is_unknown, is_free
+
+    def last_query_ms(self) -> float:
+        """Device time of the last lookup kernel (maps created with FLAG_TIMING)."""
+        out = C.c_float()
+        self._check(self.lib.bxg_pmap_last_query_ms(self.h, C.byref(out)))
+        return out.value
 
     def active_cells_count(self) -> int:
         out = C.c_size_t()

@@ -160,6 +160,7 @@ struct bxg_pmap_s {
   uint64_t cast_ub = 0;      // upper bound of queued rays on the device
   uint64_t last_stats[8] = {0};
   float last_times[4] = {0};
+  float last_query_ms = 0;       // device time of the last lookup kernel (BXG_FLAG_TIMING)
   uint32_t last_new_leaves = 0;  // leaves created by the last scan (pool headroom)
   double dir_reach = 0;          // cells of the coming ray phase lie within this range
   uint32_t dir_epoch = 0;        // leaf-directory epoch of the last scan (1..15)

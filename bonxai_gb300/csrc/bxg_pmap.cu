@@ -732,13 +732,17 @@ int query(bxg_pmap m_, const int32_t* xyz, size_t n, uint8_t* out, int mode) {
   if (st) return st;
   st = stage_out(m, m->s_out, out, n, &dout);
   if (st) return st;
+  record(m_, 0);
   k_query<<<unsigned((n + 255) / 256), 256, 0, m->stream>>>(
       m->dm, static_cast<const int32_t*>(dxyz), uint32_t(n), mode,
       m_->opt.occupancy_threshold_log, static_cast<uint8_t*>(dout));
   BXG_LAUNCHED(m);
+  record(m_, 1);
   st = stage_out_finish(m, out, dout, n);
   if (st) return st;
   BXG_CUDA(m, cudaStreamSynchronize(m->stream));
+  if ((m->flags & BXG_FLAG_TIMING) && m_->ev[0] && m_->ev[1])
+    cudaEventElapsedTime(&m_->last_query_ms, m_->ev[0], m_->ev[1]);
   return BXG_OK;
 }
 
@@ -969,6 +973,12 @@ int bxg_pmap_synchronize(bxg_pmap m) {
 int bxg_pmap_last_stats(bxg_pmap m, uint64_t out[8]) {
   if (!m || !out) return BXG_ERR_INVALID_ARG;
   std::memcpy(out, m->last_stats, sizeof(m->last_stats));
+  return BXG_OK;
+}
+
+int bxg_pmap_last_query_ms(bxg_pmap m, float* ms) {
+  if (!m || !ms) return BXG_ERR_INVALID_ARG;
+  *ms = m->last_query_ms;
   return BXG_OK;
 }
 

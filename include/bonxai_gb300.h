@@ -297,6 +297,9 @@ int bxg_pmap_synchronize(bxg_pmap m);
 /* Statistics of the last scan: [0] points, [1] cast rays, [2] ray cells
  * visited, [3] cells updated by rays, [4] new leaves, [5] kernel launches. */
 int bxg_pmap_last_stats(bxg_pmap m, uint64_t out[8]);
+/* Device time (ms) of the last isOccupied / isUnknown / isFree kernel, with
+ * BXG_FLAG_TIMING (CUDA events around the kernel on the handle's stream). */
+int bxg_pmap_last_query_ms(bxg_pmap m, float* ms);
 /* With BXG_FLAG_TIMING: device milliseconds of each phase of the last scan,
  * measured with CUDA events on the handle's stream: [0] endpoints,
  * [1] endpoint winners, [2] endpoint update, [3] rays. */

@@ -287,6 +287,8 @@ def test_kernel_timing_and_stats(gpu, port):
     assert st["points"] == 20000 and st["ray_cells_visited"] == v - 20000
     t = m.kernel_times()
     assert all(x >= 0 for x in t) and t[3] > 0
+    m.is_occupied(np.zeros((50000, 3), np.int32))
+    assert m.last_query_ms() > 0
 
 
 def _adversarial_points(res, origin, max_range, n, seed):
