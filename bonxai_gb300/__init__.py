@@ -185,17 +185,19 @@ def _in(a, dtype, cols=None):
         n = t.shape[0] if t.dim() else 1
         return C.c_void_p(t.data_ptr()), t, n
     arr = np.ascontiguousarray(a, dtype=dtype)
-    if cols:
+    if cols and (arr.ndim != 2 or arr.shape[1] != cols):
         arr = arr.reshape(-1, cols)
-    return arr.ctypes.data_as(_vp), arr, (arr.shape[0] if arr.ndim else 1)
+    # the address as a plain int: the c_void_p argtypes take it as is, and it
+    # is cheaper than building a ctypes pointer object per call
+    return arr.ctypes.data, arr, (arr.shape[0] if arr.ndim else 1)
 
 
 def _ptr(arr):
     if arr is None:
         return None
     if _is_torch(arr):
-        return C.c_void_p(arr.data_ptr())
-    return arr.ctypes.data_as(_vp)
+        return arr.data_ptr()
+    return arr.ctypes.data
 
 
 class _Handle:
@@ -420,8 +422,10 @@ class ProbabilisticMap(_Handle):
 
     def insert_point_cloud(self, points, origin, max_range: float, stride: int = 0) -> int:
         """insertPointCloud; returns V = points + cast ray cells."""
-        is64 = (getattr(points, "dtype", None) == np.float64 or
-                str(getattr(points, "dtype", "")) == "torch.float64")
+        if isinstance(points, np.ndarray):
+            is64 = points.dtype == np.float64
+        else:
+            is64 = str(getattr(points, "dtype", "")) == "torch.float64"
         dt = np.float64 if is64 else np.float32
         p, keep, n = _in(points, dt, None if stride else 3)
         o = np.ascontiguousarray(np.asarray(origin, dt).reshape(3))
