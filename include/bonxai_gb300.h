@@ -59,10 +59,11 @@ typedef struct {
   float hash_load_factor;   /* grow the root hash above this load; 0 = 0.5 */
   int device;               /* CUDA device ordinal; -1 = current */
   void* stream;             /* cudaStream_t to run on; NULL = a stream of its own */
-  uint32_t rays_per_warp;   /* ray kernel: rays per warp 1, 2 or 4; 0 = autotuned */
-  uint32_t block_size;      /* ray kernel threads per block; 0 = autotuned */
+  uint32_t rays_per_warp;   /* ray kernel: rays per warp 1, 2 or 4; 0 = 1 */
+  uint32_t block_size;      /* ray kernel threads per block (64..256); 0 = 256 */
   uint32_t flags;           /* BXG_FLAG_* */
-  uint32_t ray_unroll;      /* ray kernel: cells per lane per step, 1 or 2; 0 = autotuned */
+  uint32_t ray_unroll;      /* ray kernel: cells per lane per step, 1 or 2; 0 = 1 */
+  /* (the defaults are what python -m bonxai_gb300.autotune picks on a GB300) */
 } bxg_config;
 
 /* Drop points with a NaN or infinite coordinate before insertion, as the
