@@ -552,7 +552,8 @@ def run_depth(args):
     m = bx.ProbabilisticMap(room.resolution,
                             bx.Config(flags=bx.FLAG_TIMING | args.flags,
                                       rays_per_warp=args.rays_per_warp,
-                                      ray_unroll=args.ray_unroll, initial_leaves=1 << 18))
+                                      ray_unroll=args.ray_unroll, block_size=args.block_size,
+                                      initial_leaves=1 << 18))
     for k in range(args.warmup):
         m.insert_point_cloud(*d_frames[k], room.max_range)
     m.clear()

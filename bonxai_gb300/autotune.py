@@ -3,7 +3,8 @@
 Tunable knobs (none changes a result, only speed):
   rays_per_warp   1, 2, 4   lanes per ray = 32 / rays_per_warp
   ray_unroll      1, 2      cells per lane per step
-  block_size      128, 256  threads per block of the per-map ray kernel
+  block_size      0, 256, 1024  threads per block of the per-map ray kernel
+                  (0: 1024 for large scans, 256 for small ones)
   hash_load_factor 0.25, 0.5, 0.75  root-hash growth threshold
 
 For each candidate the tuner replays a short sample of the workload on fresh
@@ -40,7 +41,7 @@ def tune_per_map(scans, resolution, max_range, repeats=2):
     import bonxai_gb300 as bx
     dev = [(torch.from_numpy(p).cuda(), o) for p, o in scans]
     results = []
-    for rpw, unroll, bs, lf in itertools.product((1, 2, 4), (1, 2), (128, 256), (0.25, 0.5, 0.75)):
+    for rpw, unroll, bs, lf in itertools.product((1, 2, 4), (1, 2), (0, 256, 1024), (0.25, 0.5, 0.75)):
         best = None
         for _ in range(repeats):
             cfg = bx.Config(rays_per_warp=rpw, ray_unroll=unroll, block_size=bs,

@@ -74,6 +74,9 @@ struct MapCore {
   size_t budget = 0;
   float load_factor = 0.5f;
   uint32_t rays_per_warp = 0, block_size = 0, ray_unroll = 0;
+  // ray kernel launch shape: block size and one resident wave of blocks
+  int ray_wave_bs[2] = {0, 0};
+  uint32_t ray_wave_blocks[2] = {0, 0};
 
   // pools
   DevBuf buckets, ichild, imask, lmask, ldata, lkey, lfree, ctr;

@@ -60,7 +60,9 @@ typedef struct {
   int device;               /* CUDA device ordinal; -1 = current */
   void* stream;             /* cudaStream_t to run on; NULL = a stream of its own */
   uint32_t rays_per_warp;   /* ray kernel: rays per warp 1, 2 or 4; 0 = 1 */
-  uint32_t block_size;      /* ray kernel threads per block (64..256); 0 = 256 */
+  uint32_t block_size;      /* ray kernel threads per block, 64..1024 (256 at most with
+                               ray_unroll 2); 0 = 1024 for scans of at least
+                               2 x SMs x 32 x rays_per_warp points, else 256 */
   uint32_t flags;           /* BXG_FLAG_* */
   uint32_t ray_unroll;      /* ray kernel: cells per lane per step, 1 or 2; 0 = 1 */
   /* (the defaults are what python -m bonxai_gb300.autotune picks on a GB300) */
