@@ -209,6 +209,9 @@ class _Handle:
             raise BonxaiError(st, msg.decode() if msg else "")
 
     def close(self):
+        if getattr(self, "_owner", None) is not None:  # a borrowed view
+            self.h = None
+            return
         if getattr(self, "h", None):
             getattr(self.lib, self._destroy)(self.h)
             self.h = None
@@ -582,6 +585,18 @@ class ProbabilisticMap(_Handle):
 
     def clear(self):
         self._check(self.lib.bxg_pmap_clear(self.h))
+
+    def grid(self) -> VoxelGrid:
+        """grid() (probabilistic_map.hpp:70-72): the map's own VoxelGrid<CellT>,
+        its values the packed int32 CellT word. A borrowed view: valid while
+        this map lives; closing it leaves the map alone."""
+        g = VoxelGrid.__new__(VoxelGrid)
+        g.lib = self.lib
+        g.dtype = np.dtype(np.int32)
+        g.voxel_size = self.resolution
+        g._owner = self
+        g.h = self.lib.bxg_pmap_grid(self.h)
+        return g
 
     def synchronize(self):
         self._check(self.lib.bxg_pmap_synchronize(self.h))

@@ -335,6 +335,7 @@ int core_init(MapCore* m, double res, int ib, int lb, size_t esz, const bxg_conf
 }
 
 int core_clear(MapCore* m) {
+  m->leaf_gen++;
   BXG_CUDA(m, cudaMemsetAsync(m->buckets.p, 0xFF, (size_t(m->dm.hmask) + 1) * 16, m->stream));
   BXG_CUDA(m, cudaMemsetAsync(m->ichild.p, 0xFF, size_t(m->dm.icap) * m->dm.isize * 4,
                               m->stream));

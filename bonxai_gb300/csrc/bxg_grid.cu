@@ -695,6 +695,7 @@ int bxg_grid_release_unused(bxg_grid g) {
   int st = core_sync(m);
   if (st) return st;
   const uint32_t nl = m->h_ctr[C_LEAF];
+  m->leaf_gen++;  // released slots are handed out again at other coordinates
   if (nl) {
     k_release_leaves<<<(nl + 255) / 256, 256, 0, m->stream>>>(m->dm, nl);
     BXG_LAUNCHED(m);

@@ -74,6 +74,9 @@ struct MapCore {
   size_t budget = 0;
   float load_factor = 0.5f;
   uint32_t rays_per_warp = 0, block_size = 0, ray_unroll = 0;
+  // bumped whenever leaf slots may be released (clear, releaseUnusedMemory):
+  // caches of coordinate -> slot built before are stale after it
+  uint64_t leaf_gen = 0;
   // ray kernel launch shape: block size and one resident wave of blocks
   int ray_wave_bs[2] = {0, 0};
   uint32_t ray_wave_blocks[2] = {0, 0};
@@ -166,7 +169,13 @@ struct bxg_pmap_s {
   float last_query_ms = 0;       // device time of the last lookup kernel (BXG_FLAG_TIMING)
   uint32_t last_new_leaves = 0;  // leaves created by the last scan (pool headroom)
   double dir_reach = 0;          // cells of the coming ray phase lie within this range
-  uint32_t dir_epoch = 0;        // leaf-directory epoch of the last scan (1..15)
+  // the leaf directory kept across scans: its cube (leaf coordinates of the
+  // corner, side), epoch (1..15) and the leaf generation it was built at
+  int dir_x0 = 0, dir_y0 = 0, dir_z0 = 0;
+  uint32_t dir_side = 0;
+  uint32_t dir_epoch = 0;
+  uint64_t dir_gen = 0;
+  bool dir_live = false;
   cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   ~bxg_pmap_s() {
     for (auto& e : ev)

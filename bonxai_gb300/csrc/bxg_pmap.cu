@@ -365,9 +365,15 @@ int launch_apply(bxg_pmap_s* pm) {
 
 namespace bxg {
 // The leaf directory for a scan from (ox, oy, oz) whose ray cells lie within
-// pm->dir_reach of the origin: a cube of leaves covering every such cell, when
-// it has at most max_words words and leaf slots fit in 28 bits. Otherwise *D
-// stays empty (the walk then probes the root hash for every leaf run).
+// pm->dir_reach of the origin: a cube of words over leaf coordinates, each
+// (epoch << 28) | leaf slot. The cube and its words are kept across scans: a
+// scan reuses them while its own cube of leaves lies inside and no leaf slot
+// was released since they were written (MapCore::leaf_gen). Otherwise a new
+// cube, centred on this origin with a margin so that a moving sensor keeps it
+// for several scans, takes the next epoch. The whole buffer is cleared when
+// the 4-bit epoch wraps, so a word of another epoch is always empty. *D stays
+// empty (the walk probes the root hash for every leaf run) when the cube would
+// exceed max_words words or leaf slots do not fit in 28 bits.
 int leaf_dir_for_scan(bxg_pmap_s* pm, int ox, int oy, int oz, LeafDir* D, size_t max_words,
                       cudaStream_t stream) {
   MapCore* m = &pm->core;
@@ -375,25 +381,41 @@ int leaf_dir_for_scan(bxg_pmap_s* pm, int ox, int oy, int oz, LeafDir* D, size_t
   *D = LeafDir{};
   if (!(pm->dir_reach > 0) || m->dm.lcap >= (1u << 28)) return BXG_OK;
   const double cells = std::ceil(pm->dir_reach * m->inv_res) + 2;
-  const double half = std::ceil(cells / double(1 << m->dm.lb)) + 1;
-  if (!(half < 128)) return BXG_OK;
-  const uint32_t side = uint32_t(2 * half + 1);
-  const size_t words = size_t(side) * side * side;
-  if (words > max_words) return BXG_OK;
-  if (m->s_dir.cap < words * 4) {
-    BXG_CUDA(m, m->s_dir.ensure(words * 4));
-    BXG_CUDA(m, cudaMemsetAsync(m->s_dir.p, 0, m->s_dir.cap, stream));
-    pm->dir_epoch = 0;
-  }
-  if (++pm->dir_epoch == 16) {  // the epoch wraps: clear once every 15 scans
-    BXG_CUDA(m, cudaMemsetAsync(m->s_dir.p, 0, words * 4, stream));
-    pm->dir_epoch = 1;
+  const double halfd = std::ceil(cells / double(1 << m->dm.lb)) + 1;
+  if (!(halfd < 128)) return BXG_OK;
+  const int half = int(halfd);
+  const int cx = ox >> m->dm.lb, cy = oy >> m->dm.lb, cz = oz >> m->dm.lb;
+  const int side_now = int(pm->dir_side);
+  auto inside = [&](int c, int lo) { return c - half >= lo && c + half < lo + side_now; };
+  const bool reuse = pm->dir_live && pm->dir_gen == m->leaf_gen && inside(cx, pm->dir_x0) &&
+                     inside(cy, pm->dir_y0) && inside(cz, pm->dir_z0);
+  if (!reuse) {
+    auto words_of = [](int h) { return size_t(2 * h + 1) * (2 * h + 1) * (2 * h + 1); };
+    int h = half + std::max(2, half / 4);
+    if (words_of(h) > max_words) h = half;
+    if (words_of(h) > max_words) return BXG_OK;
+    const size_t words = words_of(h);
+    if (m->s_dir.cap < words * 4) {
+      BXG_CUDA(m, m->s_dir.ensure(words * 4));
+      BXG_CUDA(m, cudaMemsetAsync(m->s_dir.p, 0, m->s_dir.cap, stream));
+      pm->dir_epoch = 0;
+    }
+    if (++pm->dir_epoch == 16) {  // the epoch wraps: clear every word ever written
+      BXG_CUDA(m, cudaMemsetAsync(m->s_dir.p, 0, m->s_dir.cap, stream));
+      pm->dir_epoch = 1;
+    }
+    pm->dir_x0 = cx - h;
+    pm->dir_y0 = cy - h;
+    pm->dir_z0 = cz - h;
+    pm->dir_side = uint32_t(2 * h + 1);
+    pm->dir_gen = m->leaf_gen;
+    pm->dir_live = true;
   }
   D->words = m->s_dir.as<uint32_t>();
-  D->side = side;
-  D->x0 = (ox >> m->dm.lb) - int(half);
-  D->y0 = (oy >> m->dm.lb) - int(half);
-  D->z0 = (oz >> m->dm.lb) - int(half);
+  D->side = pm->dir_side;
+  D->x0 = pm->dir_x0;
+  D->y0 = pm->dir_y0;
+  D->z0 = pm->dir_z0;
   D->epoch = pm->dir_epoch;
   return BXG_OK;
 }

@@ -256,12 +256,14 @@ __device__ __forceinline__ bool winner_apply(const DMap& M, int4 e, int32_t u, c
 // op(act, leaf, ci, k): act = the lane has a cell (k < m), leaf = its leaf
 // slot (kNone if the pool ran out), ci = its index in the leaf, k = its
 // position on the ray.
-// Leaf directory of one scan: a dense cube of `side`^3 words over the leaves
-// within max_range of the origin (x0/y0/z0: leaf coordinate of its corner).
-// A word holds (epoch << 28) | leaf slot; a word of another epoch is empty, so
-// the cube is cleared only when the 4-bit epoch wraps. A head inside the cube
-// reads one word instead of probing the root hash and the inner node, and
-// writes the slot it resolved otherwise (racing writers store the same word).
+// Leaf directory: a dense cube of `side`^3 words over the leaves around the
+// scan's origin, covering every leaf within max_range (x0/y0/z0: leaf
+// coordinate of its corner). A word holds (epoch << 28) | leaf slot; a word of
+// another epoch is empty, so the cube is cleared only when the 4-bit epoch
+// wraps. The host keeps a cube and its words across scans until the origin
+// leaves it or a leaf slot is released. A head inside the cube reads one word
+// instead of probing the root hash and the inner node, and writes the slot it
+// resolved otherwise (racing writers store the same word).
 struct LeafDir {
   uint32_t* words;  // nullptr: no directory
   int x0, y0, z0;

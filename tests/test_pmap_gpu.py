@@ -144,6 +144,48 @@ def test_leaf_directory_vs_oracle(gpu, port):
     assert_same_map(m3, o3)
 
 
+def test_leaf_directory_across_scans(gpu, port):
+    """The leaf directory kept across scans. 20 scans of a sensor moving 9.5 m
+    (its cube is re-centred once the origin leaves the margin) match the
+    oracle. Then cells are switched off and their leaves released through
+    grid(): later scans, whose new leaves reuse the released slots, match a
+    twin map rebuilt from the same state with a fresh directory."""
+    scene = synth.LidarScene()
+    m = gpu.ProbabilisticMap(scene.resolution)
+    o = port.pmap(scene.resolution)
+    for k in range(20):
+        pts, org = scene.scan(k, n_points=8192)
+        assert m.insert_point_cloud(pts, org, scene.max_range) == o.insert(pts, org, scene.max_range)
+    assert_same_map(m, o)
+
+    m2 = gpu.ProbabilisticMap(scene.resolution)
+    for k in range(5):
+        pts, org = scene.scan(k, n_points=8192)
+        m2.insert_point_cloud(pts, org, scene.max_range)
+    xyz, _ = m2.dump()
+    # every on-cell of the leaves within 7 leaves of the next origin: those
+    # leaves empty out and are released
+    _, org5 = scene.scan(5, n_points=8192)
+    c5 = np.floor(np.asarray(org5, np.float64) / scene.resolution).astype(np.int64) >> 3
+    sel = np.all(np.abs((xyz.astype(np.int64) >> 3) - c5) <= 7, axis=1)
+    assert sel.sum() > 1000
+    g = m2.grid()
+    roots0, leaves0 = g.node_counts()
+    g.set_cells_off(xyz[sel])
+    g.release_unused_memory()
+    assert g.node_counts()[1] < leaves0
+    twin = gpu.ProbabilisticMap(scene.resolution)
+    twin.grid().deserialize(g.serialize("int"))
+    while twin.update_count != m2.update_count:
+        twin.update_free_cells(np.zeros(3))
+    for k in range(5, 10):
+        pts, org = scene.scan(k, n_points=8192)
+        assert m2.insert_point_cloud(pts, org, scene.max_range) == \
+            twin.insert_point_cloud(pts, org, scene.max_range)
+    a, b = m2.dump(), twin.dump()
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+
+
 def test_depth_frames_vs_oracle(gpu, port):
     room = synth.DepthRoom()
     m = gpu.ProbabilisticMap(room.resolution)
