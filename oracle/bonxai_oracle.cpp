@@ -43,51 +43,62 @@ struct CoordHash {
 };
 
 // Bit set of 2^(3*log2dim) bits in 64-bit words (mask.hpp:19-140,255-263).
+// Up to eight words (leaf_bits <= 3, every inner node of inner_bits <= 3) live
+// inside the object, as the reference's Mask keeps them, so a mask test costs
+// no pointer chase; larger masks live on the heap.
 class Bits {
  public:
   explicit Bits(int log2dim)
-      : nbits_(1u << (3 * log2dim)), w_(std::max<uint32_t>(nbits_ >> 6, 1u), 0) {}
-  bool on(uint32_t i) const { return (w_[i >> 6] >> (i & 63)) & 1u; }
+      : nbits_(1u << (3 * log2dim)), nw_(std::max<uint32_t>(nbits_ >> 6, 1u)) {
+    if (nw_ > kInline) big_.assign(nw_, 0);
+  }
+  bool on(uint32_t i) const { return (w()[i >> 6] >> (i & 63)) & 1u; }
   // setOn / setOff return the previous state (mask.hpp:351-365).
   bool set_on(uint32_t i) {
+    uint64_t& x = w()[i >> 6];
     const uint64_t b = uint64_t(1) << (i & 63);
-    const bool was = w_[i >> 6] & b;
-    w_[i >> 6] |= b;
+    const bool was = x & b;
+    x |= b;
     return was;
   }
   bool set_off(uint32_t i) {
+    uint64_t& x = w()[i >> 6];
     const uint64_t b = uint64_t(1) << (i & 63);
-    const bool was = w_[i >> 6] & b;
-    w_[i >> 6] &= ~b;
+    const bool was = x & b;
+    x &= ~b;
     return was;
   }
   uint32_t count() const {
     uint32_t n = 0;
-    for (uint64_t w : w_) n += uint32_t(__builtin_popcountll(w));
+    for (uint32_t k = 0; k < nw_; k++) n += uint32_t(__builtin_popcountll(w()[k]));
     return n;
   }
   bool none() const {
-    for (uint64_t w : w_)
-      if (w) return false;
+    for (uint32_t k = 0; k < nw_; k++)
+      if (w()[k]) return false;
     return true;
   }
   // Calls f(i) for every set bit, lowest first (mask.hpp:154-253).
   template <class F>
   void for_each(F&& f) const {
-    for (uint32_t k = 0; k < w_.size(); k++) {
-      uint64_t w = w_[k];
-      while (w) {
-        const uint32_t b = uint32_t(__builtin_ctzll(w));
+    for (uint32_t k = 0; k < nw_; k++) {
+      uint64_t x = w()[k];
+      while (x) {
+        const uint32_t b = uint32_t(__builtin_ctzll(x));
         f((k << 6) + b);
-        w &= w - 1;
+        x &= x - 1;
       }
     }
   }
-  void clear() { std::fill(w_.begin(), w_.end(), 0); }
+  void clear() { std::fill(w(), w() + nw_, uint64_t(0)); }
 
  private:
-  uint32_t nbits_;
-  std::vector<uint64_t> w_;
+  static constexpr uint32_t kInline = 8;
+  uint64_t* w() { return nw_ <= kInline ? inl_ : big_.data(); }
+  const uint64_t* w() const { return nw_ <= kInline ? inl_ : big_.data(); }
+  uint32_t nbits_, nw_;
+  uint64_t inl_[kInline] = {0, 0, 0, 0, 0, 0, 0, 0};
+  std::vector<uint64_t> big_;
 };
 
 template <class T>
@@ -137,15 +148,29 @@ class Grid {
                     ((c.z & leaf_mask_) << (2 * lb_)));
   }
 
-  // Accessor::getLeafGrid (bonxai.hpp:588-621) without the root cache.
-  Leaf<T>* leaf(const Coord& c, bool create) {
+  // Accessor::getLeafGrid (bonxai.hpp:588-621). The caller's one-entry root
+  // cache (*rk_cache, *in_cache) skips the hash lookup while consecutive
+  // leaves share a root; node addresses of the unordered_map are stable until
+  // an erase, and every erase path resets the accessors.
+  Leaf<T>* leaf(const Coord& c, bool create, Coord* rk_cache = nullptr,
+                Inner<T>** in_cache = nullptr) {
     const Coord rk = root_key(c);
-    auto it = roots_.find(rk);
-    if (it == roots_.end()) {
-      if (!create) return nullptr;
-      it = roots_.emplace(rk, Inner<T>(ib_)).first;
+    Inner<T>* inp = nullptr;
+    if (in_cache && *in_cache && *rk_cache == rk) {
+      inp = *in_cache;
+    } else {
+      auto it = roots_.find(rk);
+      if (it == roots_.end()) {
+        if (!create) return nullptr;
+        it = roots_.emplace(rk, Inner<T>(ib_)).first;
+      }
+      inp = &it->second;
+      if (in_cache) {
+        *in_cache = inp;
+        *rk_cache = rk;
+      }
     }
-    Inner<T>& in = it->second;
+    Inner<T>& in = *inp;
     const uint32_t ii = inner_index(c);
     if (create) {
       if (!in.bits.set_on(ii)) in.child[ii].reset(new Leaf<T>(lb_));
@@ -224,15 +249,15 @@ class Access {
   void reset() {
     has_ = false;
     leaf_ = nullptr;
+    inner_ = nullptr;
   }
+  // The cache test is inline; the lookup behind it is out of line, as the
+  // reference keeps getLeafGrid behind its inline key comparison
+  // (bonxai.hpp:476-481).
   Leaf<T>* leaf_for(const Coord& c, bool create) {
     const Coord k = g_.leaf_key(c);
-    if (!has_ || k != key_ || (create && leaf_ == nullptr)) {
-      leaf_ = g_.leaf(c, create);
-      key_ = k;
-      has_ = true;
-    }
-    return leaf_;
+    if (has_ && k == key_ && !(create && leaf_ == nullptr)) return leaf_;
+    return refill(c, k, create);
   }
   // setValue (bonxai.hpp:449-466): returns the previous on-state.
   bool set_value(const Coord& c, const T& v) {
@@ -269,10 +294,19 @@ class Access {
   }
 
  private:
+  __attribute__((noinline)) Leaf<T>* refill(const Coord& c, const Coord& k, bool create) {
+    leaf_ = g_.leaf(c, create, &root_, &inner_);
+    key_ = k;
+    has_ = true;
+    return leaf_;
+  }
+
   Grid<T>& g_;
   bool has_ = false;
   Coord key_{0, 0, 0};
   Leaf<T>* leaf_ = nullptr;
+  Coord root_{0, 0, 0};
+  Inner<T>* inner_ = nullptr;
 };
 
 // RayIterator (probabilistic_map.hpp:162-203): integer 3D Bresenham that visits
@@ -361,17 +395,24 @@ class PMap {
   uint64_t update_free_cells(double ox, double oy, double oz) {
     Access<int32_t> acc(grid_);
     const Coord o = grid_.pos_to_coord(ox, oy, oz);
+    // a ray visits chebyshev(o, e) cells (none when e == o), so the count of
+    // visited cells is summed per ray rather than per cell
     uint64_t visited = 0;
     auto clear_point = [&](const Coord& c) {
       int32_t* w = acc.value(c, true);
       if (cell_id(*w) != update_count) {
         *w = cell_pack(std::max(wrap_add(cell_prob(*w), miss), cmin), update_count);
       }
-      visited++;
     };
-    for (const Coord& e : hits_) walk_ray(o, e, clear_point);
+    for (const Coord& e : hits_) {
+      visited += uint64_t(chebyshev(o, e));
+      walk_ray(o, e, clear_point);
+    }
     hits_.clear();
-    for (const Coord& e : misses_) walk_ray(o, e, clear_point);
+    for (const Coord& e : misses_) {
+      visited += uint64_t(chebyshev(o, e));
+      walk_ray(o, e, clear_point);
+    }
     misses_.clear();
     if (++update_count == 4) update_count = 1;
     return visited;

@@ -47,13 +47,16 @@ def build_port(force: bool = False) -> Path:
     return PORT_SO
 
 
-def build_ref() -> Path | None:
-    """Build oracle/_ref from the mounted reference sources, if present."""
+def build_ref(ref_root: str | None = None) -> Path | None:
+    """Build oracle/_ref with the recipe oracle/build_ref.sh. The reference root
+    is the argument, else $BONXAI_REFERENCE, else the recipe's own default; the
+    recipe skips the build (exit 0) where the sources are not mounted."""
     script = HERE / "build_ref.sh"
-    ref_root = os.environ.get("BONXAI_REFERENCE", "/root/reference")
-    if not (Path(ref_root) / "bonxai_map" / "src" / "probabilistic_map.cpp").exists():
-        return None
-    subprocess.check_call(["bash", str(script), ref_root])
+    cmd = ["bash", str(script)]
+    root = ref_root or os.environ.get("BONXAI_REFERENCE")
+    if root:
+        cmd.append(root)
+    subprocess.check_call(cmd)
     return REF_SO if REF_SO.exists() else None
 
 
