@@ -12,6 +12,7 @@
 // Items are independent after step 1, so no two threads write one cell.
 #include <algorithm>
 #include <mutex>
+#include <vector>
 
 #include "bxg_internal.h"
 
@@ -293,6 +294,37 @@ __global__ void k_hold_leaf(DMap M, int x, int y, int z, int* held) {
   if (in == kNone) return;
   uint32_t* slot = M.ichild + static_cast<size_t>(in) * M.isize + inner_index(M, x, y, z);
   if (atomicCAS(slot, kNone, kPending) == kNone) *held = 1;
+}
+
+// Accessor::getLeafGrid / ConstAccessor::getLeafGrid (bonxai.hpp:588-647)
+// for the host: copies the inner-node mask of the root holding (x, y, z) and,
+// when the leaf exists, its mask words and all its cell values into out:
+// [int flags][pad][inner mask words][leaf mask words][cells]. flags bit 0: the
+// root exists; bit 1: the leaf exists. Missing parts are written as zeros.
+__global__ void k_read_leaf(DMap M, int x, int y, int z, uint8_t* out) {
+  __shared__ uint32_t s_in, s_leaf;
+  if (threadIdx.x == 0) {
+    const int32_t rm = root_mask(M);
+    s_in = root_find(M, x & rm, y & rm, z & rm);
+    s_leaf = kNone;
+    if (s_in != kNone) {
+      const uint32_t c = M.ichild[static_cast<size_t>(s_in) * M.isize + inner_index(M, x, y, z)];
+      s_leaf = c < kPending ? c : kNone;
+    }
+    *reinterpret_cast<int*>(out) = (s_in != kNone ? 1 : 0) | (s_leaf != kNone ? 2 : 0);
+  }
+  __syncthreads();
+  const uint32_t in = s_in, lf = s_leaf;
+  unsigned long long* im = reinterpret_cast<unsigned long long*>(out + 8);
+  unsigned long long* lm = im + M.iwords;
+  uint8_t* cells = reinterpret_cast<uint8_t*>(lm + M.lwords);
+  for (int t = threadIdx.x; t < M.iwords; t += blockDim.x)
+    im[t] = in != kNone ? M.imask[static_cast<size_t>(in) * M.iwords + t] : 0ull;
+  for (int t = threadIdx.x; t < M.lwords; t += blockDim.x)
+    lm[t] = lf != kNone ? M.lmask[static_cast<size_t>(lf) * M.lwords + t] : 0ull;
+  const size_t bytes = static_cast<size_t>(M.lsize) * M.esz;
+  const uint8_t* src = M.ldata + static_cast<size_t>(lf) * bytes;
+  for (size_t t = threadIdx.x; t < bytes; t += blockDim.x) cells[t] = lf != kNone ? src[t] : 0;
 }
 
 // Builds the dedup table for n device coordinates.
@@ -735,6 +767,30 @@ int bxg_debug_hold_leaf(bxg_grid g, const int32_t xyz[3]) {
   const int st = core_sync(m);
   if (st) return st;
   if (held != 1) return set_error(m, BXG_ERR_INVALID_ARG, "the leaf exists or cannot be reached");
+  return BXG_OK;
+}
+
+int bxg_grid_read_leaf(bxg_grid g, const int32_t xyz[3], uint64_t* inner_mask,
+                       uint64_t* leaf_mask, void* cells, int* found) {
+  if (check_grid(g) || !xyz) return BXG_ERR_INVALID_ARG;
+  MapCore* m = &g->core;
+  cudaSetDevice(m->device);
+  const size_t iw = size_t(m->dm.iwords), lw = size_t(m->dm.lwords);
+  const size_t cb = size_t(m->dm.lsize) * size_t(m->dm.esz);
+  const size_t bytes = 8 + 8 * (iw + lw) + cb;
+  BXG_CUDA(m, m->s_out2.ensure(bytes));
+  k_read_leaf<<<1, 256, 0, m->stream>>>(m->dm, xyz[0], xyz[1], xyz[2], m->s_out2.as<uint8_t>());
+  BXG_LAUNCHED(m);
+  std::vector<uint8_t> h(bytes);
+  BXG_CUDA(m, cudaMemcpyAsync(h.data(), m->s_out2.p, bytes, cudaMemcpyDeviceToHost, m->stream));
+  const int st = core_sync(m);
+  if (st) return st;
+  int flags = 0;
+  std::memcpy(&flags, h.data(), sizeof(int));
+  if (found) *found = flags;
+  if (inner_mask) std::memcpy(inner_mask, h.data() + 8, 8 * iw);
+  if (leaf_mask) std::memcpy(leaf_mask, h.data() + 8 + 8 * iw, 8 * lw);
+  if (cells && cb) std::memcpy(cells, h.data() + 8 + 8 * (iw + lw), cb);
   return BXG_OK;
 }
 

@@ -181,6 +181,16 @@ typedef struct {
 } bxg_device_view;
 int bxg_grid_device_view(bxg_grid g, bxg_device_view* out);
 
+/* Accessor::getLeafGrid / ConstAccessor::getLeafGrid
+ * (bonxai_core/include/bonxai/bonxai.hpp:588-647) for host code: one leaf and
+ * the mask of its inner node, copied to host buffers (each may be NULL).
+ * inner_mask: max(2^(3*inner_bits)/64, 1) words; leaf_mask: max(2^(3*leaf_bits)/64,
+ * 1) words; cells: 2^(3*leaf_bits) values of value_bytes each, x fastest (cells
+ * whose mask bit is off read as zero bytes). *found: bit 0 set when the root
+ * (inner node) exists, bit 1 when the leaf exists; missing parts read as zero. */
+int bxg_grid_read_leaf(bxg_grid g, const int32_t xyz[3], uint64_t* inner_mask,
+                       uint64_t* leaf_mask, void* cells, int* found);
+
 /* Test hook (no counterpart in the reference): marks the leaf that would hold
  * xyz as being created by a creator that never finishes. Any later access to
  * that leaf waits out the device-side spin limit (about a second) and the call

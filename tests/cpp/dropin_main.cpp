@@ -109,6 +109,89 @@ static int tutorial(const std::string& out) {
   return 0;
 }
 
+// Walks the tree the way the reference's Serialize does
+// (bonxai_core/include/bonxai/serialization.hpp:91-113): rootMap(), the inner
+// masks, each leaf's mask and on-cell values. Checks the walk against
+// activeCellsCount / forEachCell, getLeafGrid copies against the walk, pointer
+// stability of value(), and writes through getLeafGrid and value() pointers.
+static int tree(const std::string& out) {
+  std::ofstream f(out);
+  Bonxai::VoxelGrid<int32_t> grid(0.05);
+  std::vector<Bonxai::CoordT> coords;
+  std::vector<int32_t> vals;
+  for (int i = 0; i < 3000; i++) {
+    coords.push_back({(i * 37) % 211 - 100, (i * 53) % 97 - 40, (i * 11) % 61 - 30});
+    vals.push_back(i * 7 + 1);
+  }
+  grid.setValues(coords, vals);
+  size_t roots = 0, leaves = 0, cells = 0;
+  long long vsum = 0;
+  bool leaf_copies_match = true;
+  auto ca = grid.createConstAccessor();
+  for (const auto& it : grid.rootMap()) {
+    const Bonxai::CoordT& root = it.first;
+    const auto& inner_grid = it.second;
+    roots++;
+    for (auto inner = inner_grid.mask().beginOn(); inner; ++inner) {
+      const uint32_t ii = *inner;
+      const auto& leaf_grid = *(inner_grid.cell(ii));
+      leaves++;
+      const int lb = int(grid.leafBits()), ib = int(grid.innetBits());
+      const int32_t im = (1 << ib) - 1;
+      const Bonxai::CoordT lc{root.x | int32_t((ii & im) << lb),
+                              root.y | int32_t(((ii >> ib) & im) << lb),
+                              root.z | int32_t(((ii >> (2 * ib)) & im) << lb)};
+      const auto* copy = ca.getLeafGrid(lc);
+      if (!copy || copy != ca.lastLeafGrid() || !ca.lastInnerGrid() ||
+          !(copy->mask() == leaf_grid.mask()) ||
+          !ca.lastInnerGrid()->mask().isOn(ii))
+        leaf_copies_match = false;
+      for (auto leaf = leaf_grid.mask().beginOn(); leaf; ++leaf) {
+        cells++;
+        vsum += leaf_grid.cell(*leaf);
+        if (copy && copy->cell(*leaf) != leaf_grid.cell(*leaf)) leaf_copies_match = false;
+      }
+    }
+  }
+  long long fsum = 0;
+  grid.forEachCell([&fsum](const int32_t& v, const Bonxai::CoordT&) { fsum += v; });
+  f << "walk " << (cells == grid.activeCellsCount() && vsum == fsum ? "same" : "differs") << " "
+    << roots << " " << leaves << " " << cells << "\n";
+  f << "leaf_copies " << (leaf_copies_match ? "same" : "differs") << "\n";
+  f << "missing_leaf " << (ca.getLeafGrid({5000, 5000, 5000}) == nullptr ? "nullptr" : "found")
+    << "\n";
+
+  // value(): one pointer per cell, all of them live at once
+  auto acc = grid.createAccessor();
+  std::vector<int32_t*> ptrs;
+  for (int i = 0; i < 40; i++) ptrs.push_back(acc.value(coords[i]));
+  bool stable = acc.value(coords[3]) == ptrs[3];
+  for (int i = 0; i < 40; i++) *ptrs[i] = -i - 1;
+  acc.flush();
+  std::vector<int32_t> got;
+  std::vector<uint8_t> found;
+  std::vector<Bonxai::CoordT> first(coords.begin(), coords.begin() + 40);
+  grid.values(first, got, found);
+  bool written = true;
+  for (int i = 0; i < 40; i++) written = written && found[i] && got[i] == -i - 1;
+  f << "pointers " << (stable ? "stable" : "moved") << " " << (written ? "stored" : "lost") << "\n";
+
+  // getLeafGrid(create): a new, empty leaf; a cell turned on through it
+  const Bonxai::CoordT far{4000, -4000, 800};
+  const size_t before_cells = grid.activeCellsCount();
+  auto* lg = acc.getLeafGrid(far, true);
+  const bool empty_leaf = lg && lg->mask().countOn() == 0 && grid.activeCellsCount() == before_cells;
+  const uint32_t li = grid.getLeafIndex(far);
+  lg->mask().setOn(li);
+  lg->cell(li) = 4242;
+  acc.flush();
+  const int32_t* pv = ca.value(far);
+  f << "leaf_create " << (empty_leaf ? "empty" : "not_empty") << " "
+    << (pv ? std::to_string(*pv) : std::string("nullptr")) << "\n";
+  acc.releasePointers();
+  return 0;
+}
+
 static int lidar(const std::string& in, const std::string& outdir) {
   std::ifstream f(in, std::ios::binary);
   int32_t n_scans = 0, n_points = 0;
@@ -203,6 +286,7 @@ int main(int argc, char** argv) {
   }
   try {
     tutorial(std::string(argv[2]) + "/tutorial.txt");
+    tree(std::string(argv[2]) + "/tree.txt");
     lidar(argv[1], argv[2]);
   } catch (const std::exception& e) {
     std::cerr << "error: " << e.what() << "\n";

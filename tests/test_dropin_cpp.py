@@ -73,6 +73,19 @@ def test_dropin_program_matches_oracle(dropin_exe, tmp_path, port):
     assert lines["serialization"] == "long 2 3 round_trip_ok"
     assert (tmp_path / "node.txt").read_text().split() == ["ingest", "same", "export", "same"]
 
+    # --- tree walk through rootMap() / getLeafGrid(), replayed on the oracle
+    t = dict(l.split(" ", 1) for l in (tmp_path / "tree.txt").read_text().splitlines())
+    tg = port.grid(0.05, 2, 3, 1)  # int32
+    i = np.arange(3000)
+    tc = np.stack([(i * 37) % 211 - 100, (i * 53) % 97 - 40, (i * 11) % 61 - 30], 1)
+    tg.set_values(tc.astype(np.int32), (i * 7 + 1).astype(np.int32))
+    walk = t["walk"].split()
+    assert walk[0] == "same"
+    assert [int(x) for x in walk[1:]] == [tg.root_count(), tg.leaf_count(), tg.active_cells()]
+    assert t["leaf_copies"] == "same" and t["missing_leaf"] == "nullptr"
+    assert t["pointers"] == "stable stored"
+    assert t["leaf_create"] == "empty 4242"
+
     # --- probabilistic map flow
     m = port.pmap(scene.resolution)
     for pts, org in scans:
