@@ -502,7 +502,9 @@ int bxg_batch_insert_f32(bxg_batch b, const bxg_pmap* maps, size_t n_scans, cons
   uint64_t tab_total = 0;
   for (size_t s = 0; s < n_scans; s++) tab_total += pow2_at_least(2 * (offsets[s + 1] - offsets[s]));
   const void* dpts = xyz;
-  const bool host_pts = !is_device_ptr(xyz);
+  const int pts_dev = ptr_device(xyz);
+  // points in another GPU's memory are copied like host points (never read in place)
+  const bool host_pts = pts_dev != b->device && pts_dev != kPtrManaged;
   bool realloc = false;
   auto grow = [&](DevBuf& d, size_t bytes) -> cudaError_t {
     if (bytes <= d.cap) return cudaSuccess;
@@ -518,7 +520,10 @@ int bxg_batch_insert_f32(bxg_batch b, const bxg_pmap* maps, size_t n_scans, cons
     BB_CUDA(b, cudaMallocHost(reinterpret_cast<void**>(&b->h_back), kBackBytes));
   }
   if (host_pts) {
-    BB_CUDA(b, cudaMemcpyAsync(b->pts.p, xyz, total * 12, cudaMemcpyHostToDevice, b->stream));
+    if (pts_dev >= 0)
+      BB_CUDA(b, cudaMemcpyPeerAsync(b->pts.p, b->device, xyz, pts_dev, total * 12, b->stream));
+    else
+      BB_CUDA(b, cudaMemcpyAsync(b->pts.p, xyz, total * 12, cudaMemcpyHostToDevice, b->stream));
     dpts = b->pts.p;
   }
 

@@ -135,15 +135,19 @@ MapCore::~MapCore() {
   if (own_stream && stream) cudaStreamDestroy(stream);
 }
 
-bool is_device_ptr(const void* p) {
-  if (!p) return false;
+int ptr_device(const void* p) {
+  if (!p) return kPtrHost;
   cudaPointerAttributes a;
   if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
     cudaGetLastError();
-    return false;
+    return kPtrHost;
   }
-  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+  if (a.type == cudaMemoryTypeManaged) return kPtrManaged;
+  if (a.type == cudaMemoryTypeDevice) return a.device;
+  return kPtrHost;
 }
+
+bool is_device_ptr(const void* p) { return ptr_device(p) != kPtrHost; }
 
 int set_error(MapCore* m, int status, const std::string& msg) {
   if (m) m->err = msg;
@@ -539,12 +543,16 @@ int stage_in(MapCore* m, DevBuf& buf, const void* src, size_t bytes, const void*
     *dev = src;
     return BXG_OK;
   }
-  if (is_device_ptr(src)) {
+  const int pd = ptr_device(src);
+  if (pd == m->device || pd == kPtrManaged) {
     *dev = src;
     return BXG_OK;
   }
   BXG_CUDA(m, buf.ensure(bytes));
-  BXG_CUDA(m, cudaMemcpyAsync(buf.p, src, bytes, cudaMemcpyHostToDevice, m->stream));
+  if (pd >= 0)  // memory of another GPU: copied, never dereferenced by our kernels
+    BXG_CUDA(m, cudaMemcpyPeerAsync(buf.p, m->device, src, pd, bytes, m->stream));
+  else
+    BXG_CUDA(m, cudaMemcpyAsync(buf.p, src, bytes, cudaMemcpyHostToDevice, m->stream));
   *dev = buf.p;
   return BXG_OK;
 }
@@ -554,7 +562,8 @@ int stage_out(MapCore* m, DevBuf& buf, void* dst, size_t bytes, void** dev) {
     *dev = nullptr;
     return BXG_OK;
   }
-  if (is_device_ptr(dst)) {
+  const int pd = ptr_device(dst);
+  if (pd == m->device || pd == kPtrManaged) {
     *dev = dst;
     return BXG_OK;
   }
@@ -565,7 +574,11 @@ int stage_out(MapCore* m, DevBuf& buf, void* dst, size_t bytes, void** dev) {
 
 int stage_out_finish(MapCore* m, void* dst, const void* dev, size_t bytes) {
   if (!dst || !bytes || dst == dev) return BXG_OK;
-  BXG_CUDA(m, cudaMemcpyAsync(dst, dev, bytes, cudaMemcpyDeviceToHost, m->stream));
+  const int pd = ptr_device(dst);
+  if (pd >= 0)
+    BXG_CUDA(m, cudaMemcpyPeerAsync(dst, pd, dev, m->device, bytes, m->stream));
+  else
+    BXG_CUDA(m, cudaMemcpyAsync(dst, dev, bytes, cudaMemcpyDeviceToHost, m->stream));
   BXG_CUDA(m, cudaStreamSynchronize(m->stream));
   return BXG_OK;
 }

@@ -850,6 +850,10 @@ int noalloc_table(MapCore* m, uint4** out) {
     return set_error(m, BXG_ERR_INVALID_ARG, "device ordinal out of range for the no-alloc path");
   std::lock_guard<std::mutex> lock(g_noalloc_mu);
   if (!g_noalloc_dev_ptr[m->device]) {
+    int cur = -1;
+    BXG_CUDA(m, cudaGetDevice(&cur));
+    if (cur != m->device)
+      return set_error(m, BXG_ERR_CUDA, "the grid's device is not current");
     void* p = nullptr;
     const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_dedup);
     if (e != cudaSuccess) return cuda_fail(m, e, "cudaGetSymbolAddress(g_noalloc_dedup)");
@@ -871,10 +875,15 @@ extern "C" int bxg_grid_set_values_noalloc(bxg_grid g, const int32_t* d_xyz,
                      "split the batch");
   if (!d_xyz || (m->dm.esz && !d_values))
     return set_error(m, BXG_ERR_INVALID_ARG, "null input");
-  if (!is_device_ptr(d_xyz) || (m->dm.esz && !is_device_ptr(d_values)))
+  auto on_grid_device = [m](const void* p) {
+    const int d = ptr_device(p);
+    return d == m->device || d == kPtrManaged;
+  };
+  if (!on_grid_device(d_xyz) || (m->dm.esz && !on_grid_device(d_values)))
     return set_error(m, BXG_ERR_INVALID_ARG,
-                     "bxg_grid_set_values_noalloc needs device-memory inputs");
-  cudaSetDevice(m->device);
+                     "bxg_grid_set_values_noalloc needs device-memory inputs on the grid's "
+                     "device");
+  BXG_CUDA(m, cudaSetDevice(m->device));
   uint4* tab = nullptr;
   int st = noalloc_table(m, &tab);
   if (st) return st;

@@ -100,7 +100,11 @@ struct MapCore {
   ~MapCore();
 };
 
-// Pointer kind.
+// Pointer kind: the ordinal of the GPU whose memory p is in, kPtrManaged for
+// managed memory (usable in place on any device), kPtrHost otherwise.
+constexpr int kPtrHost = -1;
+constexpr int kPtrManaged = -2;
+int ptr_device(const void* p);
 bool is_device_ptr(const void* p);
 
 int set_error(MapCore* m, int status, const std::string& msg);

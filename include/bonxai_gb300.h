@@ -110,14 +110,21 @@ int bxg_grid_set_values(bxg_grid g, const int32_t* xyz, const void* values, size
  * counterpart in the reference). For callers that cannot call cudaMalloc while
  * they run -- a real-time thread, where an allocation can block for
  * milliseconds and a free synchronises the device, or a process that reserves
- * its device memory up front. Inputs must be device memory; at most 131072
- * items per call (split larger batches: consecutive batches give the same
- * cells); the grid's node pools are not grown, so a full pool returns
- * BXG_ERR_OUT_OF_POOL (bxg_grid_set_values, or a larger initial_leaves, makes
- * room). Its scratch table is a fixed 4 MiB array that each GPU loading this
- * library holds until exit and that all calls share: calls that overlap on the
- * GPU race. The first call on each device looks up that array's device
- * address; make it before any stream capture. */
+ * its device memory up front. Inputs must be device memory of the grid's own
+ * GPU (BXG_ERR_INVALID_ARG otherwise); at most 131072 items per call (split
+ * larger batches: consecutive batches give the same cells).
+ * Nothing is grown: the node pools and the root hash keep the sizes they have.
+ * A full leaf or inner pool returns BXG_ERR_OUT_OF_POOL; a root hash past its
+ * capacity returns BXG_ERR_HASH_FULL (create the grid with hash_buckets of at
+ * least twice the roots it will hold, and initial_leaves / initial_inners for
+ * its leaves, or let bxg_grid_set_values grow them first). A call that fails
+ * may have written part of its batch; running the same batch again (here or
+ * through bxg_grid_set_values, after room is made) gives the same grid as one
+ * successful call.
+ * Its scratch table is a fixed 4 MiB array that each GPU loading this library
+ * holds until exit and that all calls share: calls that overlap on the GPU
+ * race. The first call on each device looks up that array's device address;
+ * make it before any stream capture. */
 int bxg_grid_set_values_noalloc(bxg_grid g, const int32_t* d_xyz, const void* d_values,
                                 size_t n);
 /* setValue(posToCoord(p), value) with float/double points (stride in bytes, 0 =
