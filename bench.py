@@ -1,31 +1,40 @@
 #!/usr/bin/env python3
 """Benchmark of the ProbabilisticMap scan path on one GB300.
 
-Workload (default ``lidar``): ProbabilisticMap::insertPointCloud of a 64-beam x
-2048-column LiDAR (131,072 float32 points per scan, elevation -25..+15 deg) in a
-seeded 40x40x8 m scene of 200 boxes, 20 scans along a straight trajectory
-(0.5 m steps), resolution 0.1 m, max range 30 m, default Options. One step is
-one scan; the map is cleared every 20 scans (outside the timed region) so the
-timed steps replay the 20-scan sequence.
+Workload (default ``multimap``): 64 independent ProbabilisticMaps of uneven
+size, each receiving one insertPointCloud scan per tick -- points per map
+log-uniform in [10k, 500k], drawn from the room and LiDAR generators,
+resolutions cycling 0.02 / 0.05 / 0.1 m, max range 10 m, default Options --
+for 50 ticks (``--steps``). Every tick runs through the batched form (one
+graph-replayed persistent launch for all 64 scans) and through the plain
+per-scan path (64 synchronous insertPointCloud calls) on identical inputs; the
+two sets of maps are compared bit-exactly after the run.
 
 Metric: ray-cell updates/s, V / t with V = points + sum of cast ray lengths
 (the count the reference's own loop performs, identical on CPU and GPU).
 
-* ``value``: device time of the whole scan (first to last kernel, CUDA events
-  on the library's stream) with the points already in HBM; L2 is flushed
-  (256 MiB write) before every timed scan.
-* ``e2e``: the same scans through the C ABI with pinned host buffers: the
-  host->device copy of the points, all kernels, and the device->host read of
-  the scan's counters, timed on the host around the call.
-* ``roofline``: the ray kernel (dominant), algorithmic bytes per launch over its
-  CUDA-event duration, against the measured HBM copy bandwidth.
-* ``cpu_baseline``: the CPU oracle (a restatement of the reference, one thread)
-  on a bounded sample of the same sequence.
+* ``value``: batched ticks, device time (CUDA events around the tick on the
+  batch's stream), points resident in HBM, L2 flushed (256 MiB write) before
+  every tick. ``plain_per_scan_value`` is the same for the per-scan path
+  (summed device time of its scans) and ``batched_over_plain`` their ratio;
+  ``wall`` gives both timed on the host around the calls.
+* ``e2e``: the batched ticks from pinned host memory through the C ABI
+  (host->device copy of the points and read-back of the counters inside).
+* ``tick_ms_p50`` / ``tick_ms_p99``: latency of one batched tick call.
+* ``roofline``: k_tick, algorithmic bytes per tick over its event-timed
+  duration, against the measured HBM copy bandwidth.
+* ``cpu_baseline``: the CPU path (the oracle restatement, timed against the
+  reference in profiles/cpu_port_vs_ref.md) on all host cores, whole maps
+  per process, one tick or more.
 
-``--impl reference`` times that CPU implementation alone on this workload.
-Under torchrun with N > 1 each rank runs an independent replica of the map
-(the scan of one map does not shard); ``value`` sums the ranks' ray-cell
-updates over the slowest rank's time.
+Other workloads (``--workload``): ``lidar`` (one map, 64x2048 LiDAR scans),
+``depth`` (640x480 depth frames, then 1 M isOccupied), ``room``
+(VoxelGrid<float> create/update/iterate), ``serve`` (32 Poisson clients).
+
+``--impl reference`` times the CPU path alone on the same workload (all host
+cores for ``multimap``). Under torchrun with N > 1 the maps are sharded
+across ranks (``multimap``) or each rank runs a replica (``lidar``); ``value``
+sums the ranks' ray-cell updates over the slowest rank's time.
 """
 from __future__ import annotations
 
@@ -648,15 +657,22 @@ def run_depth(args):
 MM_RANGE = 10.0
 
 
-def multimap_inputs(n_maps: int):
+def multimap_inputs(n_maps: int, only=None, max_points=None):
     """Base scan per map (log-uniform 10k..500k points, room or LiDAR
     generator, resolution cycling 0.02/0.05/0.1 m). Tick t moves a LiDAR
     sensor 0.5 m along +x (five poses, cycling) and re-observes a room from
-    its centre."""
+    its centre. `only`: indices of the maps to generate (None: all); the
+    others get None. `max_points` caps the points per map (small test runs)."""
     from bonxai_gb300 import synth
     specs = synth.multi_map_specs(n_maps)
+    if max_points:
+        for sp in specs:
+            sp.n_points = min(sp.n_points, int(max_points))
     base = []
     for sp in specs:
+        if only is not None and sp.index not in only:
+            base.append(None)
+            continue
         if sp.kind == "lidar":
             n_az = max(16, -(-sp.n_points // 64))
             scene = synth.LidarScene(seed=sp.seed, n_az=n_az, max_range=MM_RANGE)
@@ -668,59 +684,191 @@ def multimap_inputs(n_maps: int):
     return specs, base
 
 
+def multimap_scan(sp, base_scan, t):
+    pts, o = base_scan
+    if sp.kind == "lidar":
+        d = np.array([0.5 * (t % 5), 0.0, 0.0], np.float32)
+        return pts + d, o + d
+    return pts, o
+
+
 def multimap_tick(specs, base, t):
-    scans = []
-    for sp, (pts, o) in zip(specs, base):
-        if sp.kind == "lidar":
-            d = np.array([0.5 * (t % 5), 0.0, 0.0], np.float32)
-            scans.append((pts + d, o + d))
-        else:
-            scans.append((pts, o))
-    return scans
+    return [multimap_scan(sp, b, t) for sp, b in zip(specs, base)]
 
 
-def _mm_cpu_worker(job):
-    """One CPU process of the map-parallel baseline: inserts its maps' scans
-    with the oracle (single-threaded per map). Returns (ray cells, seconds)."""
+def _farm_worker(conn, n_maps, mine, max_points):
+    """One CPU process of the map-parallel CPU path: owns the maps `mine`
+    (oracle maps, single-threaded each, persistent across ticks) and inserts
+    their scans of the ticks it is sent."""
     from oracle import oracle as O
     port = O.port()
-    V, dt = 0, 0.0
-    for res, pts, o in job:
-        m = port.pmap(res)
-        t0 = time.perf_counter()
-        V += m.insert(pts, o, MM_RANGE)
-        dt += time.perf_counter() - t0
-    return V, dt
+    specs, base = multimap_inputs(n_maps, only=set(mine), max_points=max_points)
+    maps = {i: port.pmap(specs[i].resolution) for i in mine}
+    ticks = {i: 0 for i in mine}
+    conn.send(("ready", 0, 0.0))
+    while True:
+        msg = conn.recv()
+        if msg is None:
+            break
+        V, dt = 0, 0.0
+        for i in msg:
+            if i not in maps:
+                continue
+            pts, o = multimap_scan(specs[i], base[i], ticks[i])
+            t0 = time.perf_counter()
+            V += maps[i].insert(pts, o, MM_RANGE)
+            dt += time.perf_counter() - t0
+            ticks[i] += 1
+        conn.send(("done", V, dt))
 
 
-def mm_cpu_baseline(specs, scans, cores):
-    """The 64 maps' first tick on the host cores, maps spread over `cores`
-    processes (spawned: the GPU is already in use in this process)."""
-    import multiprocessing as mp
-    order = sorted(range(len(specs)), key=lambda i: -len(scans[i][0]))
-    jobs = [[] for _ in range(cores)]
-    load = [0] * cores
-    for i in order:  # longest first onto the least-loaded process
-        k = min(range(cores), key=lambda c: load[c])
-        jobs[k].append((specs[i].resolution, scans[i][0], scans[i][1]))
-        load[k] += len(scans[i][0])
-    with mp.get_context("spawn").Pool(cores) as pool:
+class MapFarm:
+    """The multi-map workload on the host cores: `cores` spawned processes,
+    whole maps assigned by longest-processing-time on their point counts
+    (bonxai_gb300.sharding), each map's scans inserted in order by the CPU
+    oracle (the reference's scan is single-threaded per map; maps are
+    independent, so they run in parallel)."""
+
+    def __init__(self, n_maps: int, cores: int, max_points=None):
+        import multiprocessing as mp
+        from bonxai_gb300 import sharding, synth
+        specs = synth.multi_map_specs(n_maps)
+        ranks = sharding.assign_maps([sp.n_points for sp in specs], cores)
+        ctx = mp.get_context("spawn")  # the GPU may be in use in this process
+        self.procs, self.conns = [], []
+        self.n_maps = n_maps
+        for r in range(cores):
+            mine = [i for i, k in enumerate(ranks) if k == r]
+            if not mine:
+                continue
+            a, b = ctx.Pipe()
+            p = ctx.Process(target=_farm_worker, args=(b, n_maps, mine, max_points), daemon=True)
+            p.start()
+            self.procs.append(p)
+            self.conns.append(a)
+        for c in self.conns:
+            c.recv()
+        self.cores = len(self.procs)
+
+    def tick(self, maps=None):
+        """Inserts the next scan of each map in `maps` (default all); returns
+        (ray-cell updates, wall seconds, summed single-core seconds)."""
+        ids = list(range(self.n_maps)) if maps is None else list(maps)
         t0 = time.perf_counter()
-        res = pool.map(_mm_cpu_worker, [j for j in jobs if j])
+        for c in self.conns:
+            c.send(ids)
+        res = [c.recv() for c in self.conns]
         wall = time.perf_counter() - t0
-    V = sum(r[0] for r in res)
-    busy = max(r[1] for r in res)
-    return {"value": V / busy, "unit": "ray-cell updates/s", "cores": cores, "kind": "port",
-            "sample": f"tick 0 of all {len(specs)} maps, maps spread over {cores} processes "
-                      f"(slowest process {busy:.1f} s, {wall:.1f} s with start-up); one core: "
-                      f"{V / sum(r[1] for r in res):.4g} ray-cell updates/s"}
+        return sum(r[1] for r in res), wall, sum(r[2] for r in res)
+
+    def close(self):
+        for c in self.conns:
+            try:
+                c.send(None)
+            except (BrokenPipeError, OSError):
+                pass
+        for p in self.procs:
+            p.join(timeout=10)
+
+
+def mm_cpu_baseline(n_maps, cores, seconds, max_points=None):
+    """cpu_baseline of the multi-map workload: whole ticks of all maps on the
+    host cores until about `seconds` of wall time (at least one tick)."""
+    farm = MapFarm(n_maps, cores, max_points)
+    try:
+        V, wall, busy, ticks = 0, 0.0, 0.0, 0
+        while wall < seconds or ticks == 0:
+            v, w, b = farm.tick()
+            V, wall, busy, ticks = V + v, wall + w, busy + b, ticks + 1
+    finally:
+        farm.close()
+    return {"value": V / wall, "unit": "ray-cell updates/s", "cores": farm.cores,
+            "kind": "port",
+            "sample": f"{ticks} tick(s) of all {n_maps} maps, maps spread over {farm.cores} "
+                      f"processes, {wall:.1f} s wall; single-core rate "
+                      f"{V / busy:.4g} ray-cell updates/s ({busy:.1f} s of one-core work). "
+                      "The port's timing is within 10 % of the reference compiled unmodified "
+                      "(profiles/cpu_port_vs_ref.md)"}
+
+
+def run_reference_multimap(args):
+    """The multi-map workload on the host's CPU cores through the CPU path
+    (the reference's algorithm as the oracle restates it): rank 0 only. Each
+    step is one tick of a rotating subset of the maps, sized so that the whole
+    run stays within a few minutes; every map still gets its scans in order."""
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    cores = os.cpu_count() or 1
+    farm = MapFarm(args.maps, cores, args.max_points)
+    try:
+        _, w0, _ = farm.tick()  # one full tick: also sizes the per-step sample
+        n_steps = args.steps + args.warmup
+        per_step = max(1, min(args.maps, int(args.maps * 150.0 / max(w0 * n_steps, 1e-9))))
+        order = list(range(args.maps))
+        cursor = 0
+
+        def subset():
+            nonlocal cursor
+            ids = [order[(cursor + k) % args.maps] for k in range(per_step)]
+            cursor = (cursor + per_step) % args.maps
+            return ids
+
+        for _ in range(args.warmup):
+            farm.tick(subset())
+        V, wall, busy = 0, 0.0, 0.0
+        for _ in range(args.steps):
+            v, w, b = farm.tick(subset())
+            V, wall, busy = V + v, wall + w, busy + b
+    finally:
+        farm.close()
+    value = V / wall
+    line = {
+        "impl": "reference", "metric": "ray-cell updates/s (64-map batched tick)",
+        "value": value, "unit": "ray-cell updates/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * wall / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+        "config": multimap_config(args, ws),
+        "cpu_baseline": {"value": value, "unit": "ray-cell updates/s", "cores": farm.cores,
+                         "kind": "port",
+                         "sample": f"each step one tick of {per_step} of the {args.maps} maps "
+                                   f"(rotating), maps spread over {farm.cores} processes; "
+                                   f"single-core rate {V / busy:.4g} ray-cell updates/s"},
+        "e2e": {"value": value, "unit": "ray-cell updates/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def multimap_config(args, ws):
+    return {"workload": "multimap_64_uneven", "maps": args.maps,
+            "points_per_map": "log-uniform 10k..500k (room / LiDAR generators)",
+            "resolutions_m": [0.02, 0.05, 0.1], "max_range_m": MM_RANGE,
+            "ticks": args.steps, "parallelism": f"maps sharded over {ws} rank(s)",
+            "l2": "flushed before every timed tick (256 MiB write)"}
+
+
+def mm_traffic():
+    """Per-tick DRAM and L2 figures of k_tick from the committed ncu summary."""
+    p = ROOT / "profiles" / "k_tick_multimap_traffic.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text())
+        except ValueError:
+            return None
+    return None
 
 
 def run_multimap(args):
-    """Under torchrun each rank takes whole maps (longest-processing-time
-    assignment by points, bonxai_gb300.sharding); no collective touches the
-    data, and rank 0 reports units summed over ranks over the slowest rank's
-    time."""
+    """The 64-map uneven workload: every tick, one insertPointCloud scan per
+    map, through the batched form (one graph-replayed persistent launch for
+    all maps) and through the plain per-scan path (one synchronous
+    insertPointCloud call per map) on identical inputs; the maps of the two
+    paths are compared bit-exactly after the run. Under torchrun each rank
+    takes whole maps (longest-processing-time assignment by points,
+    bonxai_gb300.sharding); no collective touches the data, and rank 0 reports
+    units summed over ranks over the slowest rank's time."""
     import torch
     import bonxai_gb300 as bx
     from bonxai_gb300 import sharding
@@ -734,7 +882,7 @@ def run_multimap(args):
         torch.cuda.set_device(0)
     dev = torch.device("cuda", torch.cuda.current_device())
     t0 = time.perf_counter()
-    specs, base = multimap_inputs(args.maps)
+    specs, base = multimap_inputs(args.maps, max_points=args.max_points)
     mine = sharding.my_maps([len(b[0]) for b in base], ws, rank)
     specs = [specs[i] for i in mine]
     base = [base[i] for i in mine]
@@ -743,14 +891,18 @@ def run_multimap(args):
         f"{sum(len(b[0]) for b in base)} of its points per tick")
     ticks = args.warmup + args.steps
     big = bx.Config(initial_leaves=1 << 16, initial_inners=1 << 12, hash_buckets=1 << 14)
+    timed_cfg = bx.Config(flags=bx.FLAG_TIMING, initial_leaves=1 << 16, initial_inners=1 << 12,
+                          hash_buckets=1 << 14)
     bmaps = [bx.ProbabilisticMap(sp.resolution, big) for sp in specs]
-    pmaps = [bx.ProbabilisticMap(sp.resolution, big) for sp in specs]
+    pmaps = [bx.ProbabilisticMap(sp.resolution, timed_cfg) for sp in specs]
     batch = bx.Batch(bx.Config(rays_per_warp=args.rays_per_warp, ray_unroll=args.ray_unroll))
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device=dev)
 
-    t_b, t_p, dev_b, V_b, V_p = 0.0, 0.0, 0.0, 0, 0
-    lat = []
+    t_b, t_p, dev_b, dev_p, V_b, V_p = 0.0, 0.0, 0.0, 0.0, 0, 0
+    lat_b, lat_p, dev_ticks = [], [], []
     phases = {}
+    alg = {"points": 0, "rays": 0, "ray_cells_updated": 0, "new_leaves": 0}
+    leaves_prev = [0] * n_maps
     launches0 = batch.stats()["launches"]
     clk = ClockSampler(dev.index)
     clk.__enter__()
@@ -771,21 +923,33 @@ def run_multimap(args):
             t_b += dt
             bst = batch.stats()
             dev_b += bst["device_ms"] / 1e3
+            dev_ticks.append(bst["device_ms"])
             for k, v in bst["phase_ms"].items():
                 phases[k] = phases.get(k, 0.0) + v / args.steps
             V_b += int(rc.sum())
-            lat.append(dt * 1e3)
+            lat_b.append(dt * 1e3)
+            for i, m in enumerate(bmaps):
+                st = m.last_stats()
+                alg["points"] += st["points"]
+                alg["rays"] += st["cast_rays"]
+                alg["ray_cells_updated"] += st["ray_cells_updated"]
+                alg["new_leaves"] += max(st["leaves"] - leaves_prev[i], 0)
+        for i, m in enumerate(bmaps):
+            leaves_prev[i] = m.last_stats()["leaves"]
         # plain per-scan path, same inputs
         flush.fill_(t)
         torch.cuda.synchronize()
         a = time.perf_counter()
-        vp = 0
+        vp, dp = 0, 0.0
         for i in range(n_maps):
             vp += pmaps[i].insert_point_cloud(dev_scans[i], org[i], MM_RANGE)
+            dp += sum(pmaps[i].kernel_times())
         dt = time.perf_counter() - a
         if timed:
             t_p += dt
+            dev_p += dp / 1e3
             V_p += vp
+            lat_p.append(dt * 1e3)
         if rc.sum() != vp:
             raise SystemExit(f"tick {t}: batched {int(rc.sum())} != plain {vp} ray cells")
     clk.__exit__(None, None, None)
@@ -794,19 +958,23 @@ def run_multimap(args):
     same = all(np.array_equal(bmaps[i].dump()[1], pmaps[i].dump()[1]) for i in range(n_maps))
     if ws > 1:
         import torch.distributed as dist
-        V_b, t_b = sharding.aggregate(V_b, t_b)
-        V_p, t_p = sharding.aggregate(V_p, t_p)
+        V_b, dev_b = sharding.aggregate(V_b, dev_b)
+        V_p, dev_p = sharding.aggregate(V_p, dev_p)
+        _, t_b = sharding.aggregate(0, t_b)
+        _, t_p = sharding.aggregate(0, t_p)
         ok = torch.tensor([1.0 if same else 0.0], device=dev)
         dist.all_reduce(ok, op=dist.ReduceOp.MIN)
         same = bool(ok.item())
-    value = V_b / t_b
-    plain = V_p / t_p
+    value = V_b / dev_b           # batched, device-timed (inputs resident in HBM)
+    plain_dev = V_p / dev_p       # plain per-scan, summed device time of its scans
+    batched_wall = V_b / t_b      # both paths timed on the host around the calls
+    plain_wall = V_p / t_p
     # e2e: the same ticks from pinned host memory through the C ABI (the batch
     # copies the points to the device inside the call)
     e2e = None
     if not args.no_e2e:
         emaps = [bx.ProbabilisticMap(sp.resolution, big) for sp in specs]
-        t_e, V_e = 0.0, 0
+        t_e, V_e, h2d = 0.0, 0, 0
         for t in range(ticks):
             scans = multimap_tick(specs, base, t)
             hp = torch.from_numpy(np.concatenate([s[0] for s in scans])).pin_memory().numpy()
@@ -819,37 +987,56 @@ def run_multimap(args):
             if t >= args.warmup:
                 t_e += dt
                 V_e += int(rc.sum())
-        h2d = int(off[-1]) * 12
+                h2d += int(off[-1]) * 12
         if ws > 1:
             V_e, t_e = sharding.aggregate(V_e, t_e)
         e2e = {"value": V_e / t_e, "unit": "ray-cell updates/s",
-               "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": n_maps * 8}
+               "h2d_bytes_per_step": h2d // args.steps,
+               "d2h_bytes_per_step": n_maps * (8 + 4 * 32),
+               "ms_per_step": 1e3 * t_e / args.steps}
         for m in emaps:
             m.close()
     if rank != 0:
         dist.destroy_process_group()
         return 0
+    # roofline of k_tick: algorithmic bytes of the timed ticks over their
+    # event-timed device duration
+    pk, pkind = peaks()
+    tick_bytes = (12 * alg["points"] + RAY_LIST_BYTES * alg["rays"] +
+                  CELL_RMW_BYTES * (alg["rays"] + alg["ray_cells_updated"]) +
+                  LEAF_MASK_BYTES * alg["new_leaves"]) / args.steps
+    tick_ms = float(np.mean(dev_ticks))
+    ach = tick_bytes / (tick_ms / 1e3) / 1e9
+    tr = mm_traffic() or {}
+    roofline = {"kernel": "k_tick (one launch per tick)", "bound": "hbm", "achieved": ach,
+                "peak": pk, "unit": "GB/s", "frac": ach / pk, "peak_kind": pkind,
+                "traffic": tr.get("dram_bytes_per_tick"),
+                "algorithmic_bytes_per_launch": tick_bytes, "launch_ms": tick_ms,
+                "l2": tr.get("l2")}
     cpu = None
     if not args.no_cpu and ws == 1:
-        cpu = mm_cpu_baseline(specs, multimap_tick(specs, base, 0), os.cpu_count() or 1)
-    lat.sort()
+        cpu = mm_cpu_baseline(args.maps, os.cpu_count() or 1, args.cpu_seconds,
+                              args.max_points)
+    lat_b.sort()
+    lat_p.sort()
+
+    def pct(v, q):
+        return v[min(len(v) - 1, int(q * len(v)))]
+
     line = {
         "metric": "ray-cell updates/s (64-map batched tick)", "value": value,
         "unit": "ray-cell updates/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1e3 * t_b / args.steps, "higher_is_better": True, "scaling": "weak",
+        "ms_per_step": 1e3 * dev_b / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "int32", "data": "synthetic",
-        "config": {"workload": "multimap_64", "maps": args.maps,
-                   "parallelism": f"maps sharded over {ws} rank(s)",
-                   "points_per_tick_rank0": int(off[-1]), "max_range_m": MM_RANGE,
-                   "resolutions_m": [0.02, 0.05, 0.1], "sizes": "log-uniform 10k..500k",
-                   "rays_per_warp": args.rays_per_warp, "ray_unroll": args.ray_unroll,
-                   "graph": batch.stats()["graph"],
-                   "l2": "flushed before every timed tick (256 MiB write)"},
-        "plain_per_scan_value": plain, "batched_over_plain": value / plain,
-        "batched_device_value": V_b / dev_b,
-        "tick_ms_p50": lat[len(lat) // 2], "tick_ms_p99": lat[min(len(lat) - 1, int(0.99 * len(lat)))],
+        "config": dict(multimap_config(args, ws), points_per_tick_rank0=int(off[-1]),
+                       rays_per_warp=args.rays_per_warp, graph=batch.stats()["graph"]),
+        "plain_per_scan_value": plain_dev, "batched_over_plain": value / plain_dev,
+        "wall": {"batched": batched_wall, "plain_per_scan": plain_wall,
+                 "batched_over_plain": batched_wall / plain_wall},
+        "tick_ms_p50": pct(lat_b, 0.5), "tick_ms_p99": pct(lat_b, 0.99),
+        "plain_tick_ms_p50": pct(lat_p, 0.5), "plain_tick_ms_p99": pct(lat_p, 0.99),
         "maps_bit_identical_batched_vs_plain": same,
-        "tick_phase_ms": phases,
+        "tick_phase_ms": phases, "roofline": roofline,
         "e2e": e2e, "cpu_baseline": cpu, "gpu_launches": launches, "clocks": clk.summary(),
     }
     print(json.dumps(line), flush=True)
@@ -960,15 +1147,17 @@ def run_serve(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="lidar",
+    ap.add_argument("--workload", default="multimap",
                     choices=["lidar", "multimap", "serve", "room", "depth"])
     ap.add_argument("--maps", type=int, default=64)
+    ap.add_argument("--max-points", type=int, default=0,
+                    help="cap on points per map of the multimap workload (small test runs)")
     ap.add_argument("--clients", type=int, default=32)
     ap.add_argument("--rate", type=float, default=2000.0, help="offered requests/s (serve)")
-    ap.add_argument("--duration", type=float, default=20.0, help="seconds of load (serve)")
+    ap.add_argument("--duration", type=float, default=60.0, help="seconds of load (serve)")
     ap.add_argument("--budget-gb", type=int, default=40)
     ap.add_argument("--rays-per-warp", type=int, default=1)
     ap.add_argument("--ray-unroll", type=int, default=1)
@@ -984,6 +1173,8 @@ def main():
         log("warmup raised to 3")
         args.warmup = 3
     if args.impl == "reference":
+        if args.workload == "multimap":
+            return run_reference_multimap(args)
         return run_reference(args)
     if args.workload == "room":
         return run_room(args)

@@ -28,14 +28,39 @@ def test_cpu_sample_counts_ray_cells(port):
     assert V == sum(m.insert(p, o, scene.max_range) for p, o in scans)
 
 
-def test_multimap_cpu_baseline_spreads_maps(port):
+def test_multimap_farm_matches_single_process(port):
+    """The map-parallel CPU path (spawned processes owning whole maps) gives the
+    same ray-cell counts as inserting the same scans in one process, tick
+    after tick."""
     import bench
-    from bonxai_gb300 import synth
-    specs = synth.multi_map_specs(3)
-    scans = []
-    for sp in specs:
-        pts = synth.room_cloud(3000, seed=sp.seed)
-        scans.append((pts, ((synth.ROOM_LO + synth.ROOM_HI) / 2).astype(np.float32)))
-    cpu = bench.mm_cpu_baseline(specs, scans, 2)
+    specs, base = bench.multimap_inputs(3, max_points=3000)
+    maps = [port.pmap(sp.resolution) for sp in specs]
+    farm = bench.MapFarm(3, 2, max_points=3000)
+    try:
+        assert farm.cores == 2
+        for t in range(2):
+            want = sum(m.insert(*bench.multimap_scan(sp, b, t), bench.MM_RANGE)
+                       for m, sp, b in zip(maps, specs, base))
+            V, wall, busy = farm.tick()
+            assert V == want and wall > 0 and busy > 0
+    finally:
+        farm.close()
+
+
+def test_multimap_cpu_baseline_fields():
+    import bench
+    cpu = bench.mm_cpu_baseline(3, 2, 0.0, max_points=2000)
     assert cpu["kind"] == "port" and cpu["cores"] == 2 and cpu["value"] > 0
-    assert "3 maps" in cpu["sample"] and "one core" in cpu["sample"]
+    assert "3 maps" in cpu["sample"] and "single-core" in cpu["sample"]
+
+
+def test_reference_arm_multimap_line():
+    import json
+    r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference",
+                        "--maps", "3", "--max-points", "2000", "--steps", "2", "--warmup", "3"],
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    line = json.loads(r.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["value"] > 0
+    assert line["config"]["workload"] == "multimap_64_uneven"
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["cpu_baseline"]["cores"] >= 1
