@@ -137,6 +137,7 @@ _SIGS = {
     "bxg_server_insert": (_int, [_vp, C.c_uint32, _vp, _sz, _vp, _dbl, _int, _vp]),
     "bxg_server_query": (_int, [_vp, C.c_uint32, _vp, _sz, _int, _int, _vp]),
     "bxg_server_get_occupied": (_int, [_vp, C.c_uint32, _int, _vp]),
+    "bxg_server_clear": (_int, [_vp, C.c_uint32, _int, _int, _vp]),
     "bxg_server_wait": (_int, [_vp, C.c_uint64, _dbl, _vp, _vp, _sz]),
     "bxg_server_drain": (_int, [_vp, _dbl]),
     "bxg_server_stats": (_int, [_vp, _vp]),
@@ -661,7 +662,8 @@ class ServerConfig(C.Structure):
     _fields_ = [("pool_budget_bytes", C.c_size_t), ("max_scans_per_tick", C.c_uint32),
                 ("max_points_per_tick", C.c_uint64), ("max_lookups_per_tick", C.c_uint64),
                 ("device", C.c_int), ("rays_per_warp", C.c_uint32), ("ray_unroll", C.c_uint32),
-                ("flags", C.c_uint32), ("initial_leaves", C.c_uint32)]
+                ("flags", C.c_uint32), ("initial_leaves", C.c_uint32),
+                ("admission_timeout_s", C.c_double)]
 
     def __init__(self, **kw):
         super().__init__()
@@ -718,6 +720,14 @@ class Server(_Handle):
                                                      C.byref(t)))
         return t.value
 
+    def clear(self, map_id, release_memory=True, discard=False) -> int:
+        """clear(CLEAR_MEMORY) of one client's map, in its request order; with
+        release_memory its pools shrink back, freeing budget for waiting inserts."""
+        t = C.c_uint64()
+        self._check(self.lib.bxg_server_clear(self.h, int(map_id), int(release_memory),
+                                              int(discard), C.byref(t)))
+        return t.value
+
     def wait_query(self, ticket, n, timeout=120.0):
         res = ServerResult()
         out = np.zeros(max(n, 1), np.uint8)
@@ -757,7 +767,7 @@ class Server(_Handle):
         keys = ["completed", "inserts", "lookups", "occupied", "ticks", "p50_ms", "p99_ms",
                 "insert_p50_ms", "insert_p99_ms", "lookup_p50_ms", "lookup_p99_ms", "ray_cells",
                 "lookup_coords", "rejected", "busy_s", "span_s", "occupied_p50_ms",
-                "occupied_p99_ms", "pool_bytes"]
+                "occupied_p99_ms", "pool_bytes", "deferred"]
         return {k: out[i] for i, k in enumerate(keys)}
 
     def map_dump(self, map_id):

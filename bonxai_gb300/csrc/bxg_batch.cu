@@ -10,8 +10,12 @@
 //            lowest index per endpoint cell in the scan's own table
 //   phase 2  winners apply their hit/miss and join their scan's ray list
 //   phase 3  prefix sum of the ray-list lengths (one global ray index space)
-//   phase 4  groups of W lanes walk rays of all scans (walk_ray), each on its
-//            own map's pools; statistics per scan
+//   phase 4  the ray phase of all scans. Two-phase form (every map has a
+//            cube bitmap, bxg_mark.cuh): 4a blocks take tasks of consecutive
+//            rays of one scan and mark their cells in that map's bitmap; 4b
+//            groups of 16 lanes apply each map's marked leaves. Single-pass
+//            form otherwise: groups of W lanes walk rays of all scans
+//            (walk_ray), each on its own map's pools. Statistics per scan.
 //   phase 5  each map's counters are copied to one read-back block
 //
 // separated by grid barriers (bounded waits: a barrier that times out sets an
@@ -24,6 +28,7 @@
 #include <vector>
 
 #include "bxg_internal.h"
+#include "bxg_mark.cuh"
 #include "bxg_scan.cuh"
 
 namespace bxg {
@@ -40,7 +45,11 @@ constexpr size_t kOffCnt = kOffStats + kMaxTickScans * 32;       // [128] u32
 constexpr size_t kOffCtr = kOffCnt + kMaxTickScans * 4;          // [128][C_WORDS] u32
 constexpr size_t kBackBytes = kOffCtr + kMaxTickScans * C_WORDS * 4;
 constexpr size_t kOffPrefix = kBackBytes;                        // [129] u32
-constexpr size_t kMetaBytes = kOffPrefix + (kMaxTickScans + 1) * 4;
+constexpr size_t kOffTaskPrefix = kOffPrefix + (kMaxTickScans + 1) * 4;  // [129] u32
+constexpr size_t kOffChunk = kOffTaskPrefix + (kMaxTickScans + 1) * 4;   // u32
+constexpr size_t kMetaBytes = kOffChunk + 16;
+// The tick's neighbourhood of shared-memory leaves around each scan's origin.
+constexpr int kTickMarkNB = 2;
 
 struct TickScan {
   DMap M;
@@ -54,6 +63,7 @@ struct TickScan {
   uint32_t tmask;                // dedup table size - 1
   int32_t keep_nonfinite;
   int32_t pad;
+  RayCube Q;  // the map's cube bitmap (two-phase ray update)
 };
 
 static_assert(sizeof(TickScan) % 8 == 0, "TickScan is copied to shared memory in 8-byte words");
@@ -68,7 +78,9 @@ struct TickArgs {
   uint32_t* ray_prefix;       // [n_scans + 1]
   uint32_t* bar;              // barrier: arrivals, generation
   uint32_t* err;              // barrier timeout
-  uint32_t* ray_next;         // next ray a group takes in phase 4 (zeroed per tick)
+  uint32_t* ray_next;         // next ray (or mark task) taken in phase 4 (zeroed per tick)
+  uint32_t* task_prefix;      // [n_scans + 1] first mark task of each scan
+  uint32_t* chunk;            // rays per mark task
   uint32_t* ctr_out;          // [n_scans][C_WORDS]
   unsigned long long* times;  // [8] global-timer stamps at each phase boundary
   uint32_t n_scans;
@@ -137,11 +149,26 @@ __device__ __forceinline__ uint32_t scan_of_ray(const uint32_t* prefix, uint32_t
   return lo;
 }
 
-template <int W, int U>
+__device__ __forceinline__ uint32_t scan_of_task(const uint32_t* prefix, uint32_t n, uint32_t t) {
+  uint32_t lo = 0, hi = n;  // last scan with prefix <= t (scans without tasks are skipped)
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (ld_volatile(prefix + mid) <= t) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
+// MARK: phase 4 in the two-phase form (every scan has a cube). Dynamic shared
+// memory: the scan table (kMaxTickScans entries), then, with MARK, the mark
+// neighbourhood (mark_smem_words(kTickMarkNB) words).
+template <int W, int U, bool MARK>
 __global__ void __launch_bounds__(256, U == 2 ? 3 : 4) k_tick(const TickArgs* __restrict__ argp,
                                                  const TickScan* __restrict__ scans_g) {
   extern __shared__ unsigned long long smem_raw[];
   TickScan* sc = reinterpret_cast<TickScan*>(smem_raw);
+  uint32_t* smk = reinterpret_cast<uint32_t*>(smem_raw + kMaxTickScans * (sizeof(TickScan) / 8));
+  __shared__ uint32_t s_next, s_task;
+  __shared__ uint32_t s_upd[kMaxTickScans];
   const TickArgs A = *argp;
   const uint32_t ns = A.n_scans;
   {
@@ -164,6 +191,7 @@ __global__ void __launch_bounds__(256, U == 2 ? 3 : 4) k_tick(const TickArgs* __
   for (unsigned long long k = gtid; k < ns; k += gsize) {
     A.cast_cnt[k] = 0;
     for (int j = 0; j < 4; j++) A.stats[4 * k + j] = 0;
+    if (MARK) *sc[k].Q.count = 0u;
   }
   if (!grid_barrier(A.bar, A.err)) return;
   stamp(1);
@@ -229,7 +257,8 @@ __global__ void __launch_bounds__(256, U == 2 ? 3 : 4) k_tick(const TickArgs* __
   if (!grid_barrier(A.bar, A.err)) return;
   stamp(3);
 
-  // phase 3: one index space over all ray lists
+  // phase 3: one index space over all ray lists (and, with MARK, over the
+  // mark tasks: about four per block, at least 64 rays each)
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     uint32_t acc = 0;
     for (uint32_t s = 0; s < ns; s++) {
@@ -237,12 +266,67 @@ __global__ void __launch_bounds__(256, U == 2 ? 3 : 4) k_tick(const TickArgs* __
       acc += min(ld_volatile(A.cast_cnt + s), sc[s].n);
     }
     A.ray_prefix[ns] = acc;
+    if (MARK) {
+      const uint32_t chunk = max(64u, (acc + 4u * gridDim.x - 1) / (4u * gridDim.x));
+      uint32_t tacc = 0;
+      for (uint32_t s = 0; s < ns; s++) {
+        A.task_prefix[s] = tacc;
+        tacc += (A.ray_prefix[s + 1] - A.ray_prefix[s] + chunk - 1) / chunk;
+      }
+      A.task_prefix[ns] = tacc;
+      *A.chunk = chunk;
+    }
   }
   if (!grid_barrier(A.bar, A.err)) return;
   stamp(4);
 
   // phase 4: rays of all scans
-  {
+  if (MARK) {
+    // 4a: mark
+    for (int t = threadIdx.x; t < mark_smem_words(kTickMarkNB); t += blockDim.x) smk[t] = 0u;
+    const uint32_t n_tasks = ld_volatile(A.task_prefix + ns);
+    const uint32_t chunk = ld_volatile(A.chunk);
+    for (;;) {
+      __syncthreads();
+      if (threadIdx.x == 0) s_task = atomicAdd(A.ray_next, 1u);
+      __syncthreads();
+      const uint32_t t = s_task;
+      if (t >= n_tasks) break;
+      const uint32_t s = scan_of_task(A.task_prefix, ns, t);
+      const TickScan& S = sc[s];
+      const uint32_t rays = ld_volatile(A.ray_prefix + s + 1) - ld_volatile(A.ray_prefix + s);
+      const uint32_t r0 = (t - ld_volatile(A.task_prefix + s)) * chunk;
+      uint32_t visited = 0;
+      mark_rays_block<kTickMarkNB>(S.M, S.Q, A.cast + S.pt_begin, r0, min(rays, r0 + chunk),
+                                   S.ox, S.oy, S.oz, smk, &s_next, visited);
+      visited = __reduce_add_sync(0xffffffffu, visited);
+      if (lane == 0 && visited)
+        atomicAdd(A.stats + 4 * s + 2, static_cast<unsigned long long>(visited));
+    }
+    if (!grid_barrier(A.bar, A.err)) return;
+    // 4b: apply, 16 lanes per marked leaf block; each scan's list is taken in
+    // a rotated order so that its first entries do not always go to the same
+    // groups
+    for (uint32_t k = threadIdx.x; k < ns; k += blockDim.x) s_upd[k] = 0u;
+    __syncthreads();
+    {
+      const unsigned sl = lane & (kApplyGroup - 1), gbase = lane & ~unsigned(kApplyGroup - 1);
+      const unsigned gmask = ((1u << kApplyGroup) - 1u) << gbase;
+      const uint32_t gid = static_cast<uint32_t>(gtid / kApplyGroup);
+      const uint32_t ng = static_cast<uint32_t>(gsize / kApplyGroup);
+      for (uint32_t s = 0; s < ns; ++s) {
+        const TickScan& S = sc[s];
+        const uint32_t n = min(ld_volatile(S.Q.count), S.Q.cap);
+        uint32_t upd = 0;
+        for (uint32_t i = (gid + s * 977u) % ng; i < n; i += ng)
+          apply_block(S.M, S.Q, S.Q.list[i], S.u, S.o.miss, S.o.cmin, sl, gbase, gmask, upd);
+        if (upd) atomicAdd(s_upd + s, upd);
+      }
+    }
+    __syncthreads();
+    for (uint32_t k = threadIdx.x; k < ns; k += blockDim.x)
+      if (s_upd[k]) atomicAdd(A.stats + 4 * k + 3, static_cast<unsigned long long>(s_upd[k]));
+  } else {
     const unsigned sl = lane & (W - 1);
     const unsigned gbase = lane & ~(W - 1);
     const unsigned gmask = (W == 32) ? 0xffffffffu : (((1u << W) - 1u) << gbase);
@@ -310,7 +394,8 @@ struct bxg_batch_s {
   uint32_t rays_per_warp = 1;
   uint32_t ray_unroll = 1;
   int sm_count = 0;
-  int grid = 0;
+  int grid = 0;       // resident blocks of the single-pass tick
+  int grid_mark = 0;  // resident blocks of the two-phase tick
   bool use_graph = true;
   // device buffers
   DevBuf pts, ep, tab, cast, meta, params;
@@ -323,7 +408,7 @@ struct bxg_batch_s {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   bool graph_ok = false;
-  uint64_t graph_key[6] = {0};
+  uint64_t graph_key[7] = {0};
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   float last_ms = 0;
   double phase_ms[5] = {0, 0, 0, 0, 0};
@@ -363,10 +448,10 @@ uint32_t pow2_at_least(uint64_t v) {
   return p;
 }
 
-template <int W, int U>
+template <int W, int U, bool MARK>
 int occupancy_grid(bxg_batch b, size_t smem) {
   int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tick<W, U>, 256, smem) !=
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tick<W, U, MARK>, 256, smem) !=
       cudaSuccess) {
     cudaGetLastError();
     return 0;
@@ -374,10 +459,17 @@ int occupancy_grid(bxg_batch b, size_t smem) {
   return per_sm * b->sm_count;
 }
 
-template <int W, int U>
+// Dynamic shared memory of a tick: the scan table, plus the mark
+// neighbourhood in the two-phase form.
+size_t tick_smem(bool mark) {
+  return kMaxTickScans * sizeof(TickScan) +
+         (mark ? size_t(mark_smem_words(kTickMarkNB)) * 4 : 0);
+}
+
+template <int W, int U, bool MARK>
 cudaError_t launch_tick(bxg_batch b, size_t smem) {
   cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(b->grid);
+  cfg.gridDim = dim3(MARK ? b->grid_mark : b->grid);
   cfg.blockDim = dim3(256);
   cfg.dynamicSmemBytes = smem;
   cfg.stream = b->stream;
@@ -388,26 +480,27 @@ cudaError_t launch_tick(bxg_batch b, size_t smem) {
   cfg.numAttrs = 1;
   const TickArgs* a = b->params.as<TickArgs>();
   const TickScan* s = reinterpret_cast<const TickScan*>(b->params.as<uint8_t>() + 256);
-  return cudaLaunchKernelEx(&cfg, k_tick<W, U>, a, s);
+  return cudaLaunchKernelEx(&cfg, k_tick<W, U, MARK>, a, s);
 }
 
-cudaError_t launch_for(bxg_batch b, size_t smem) {
+cudaError_t launch_for(bxg_batch b, size_t smem, bool mark) {
+  if (mark) return launch_tick<32, 1, true>(b, smem);
   const bool u2 = b->ray_unroll == 2;
   switch (b->rays_per_warp) {
-    case 4: return u2 ? launch_tick<8, 2>(b, smem) : launch_tick<8, 1>(b, smem);
-    case 2: return u2 ? launch_tick<16, 2>(b, smem) : launch_tick<16, 1>(b, smem);
-    default: return u2 ? launch_tick<32, 2>(b, smem) : launch_tick<32, 1>(b, smem);
+    case 4: return u2 ? launch_tick<8, 2, false>(b, smem) : launch_tick<8, 1, false>(b, smem);
+    case 2: return u2 ? launch_tick<16, 2, false>(b, smem) : launch_tick<16, 1, false>(b, smem);
+    default: return u2 ? launch_tick<32, 2, false>(b, smem) : launch_tick<32, 1, false>(b, smem);
   }
 }
 
 // Enqueues one tick: parameters up, the persistent kernel, results back.
-cudaError_t enqueue_tick(bxg_batch b, size_t param_bytes, size_t smem) {
+cudaError_t enqueue_tick(bxg_batch b, size_t param_bytes, size_t smem, bool mark) {
   cudaError_t e = cudaMemcpyAsync(b->params.p, b->h_args, param_bytes, cudaMemcpyHostToDevice,
                                   b->stream);
   if (e != cudaSuccess) return e;
   e = cudaMemsetAsync(b->meta.p, 0, 16, b->stream);  // barrier, error and ray-counter words
   if (e != cudaSuccess) return e;
-  e = launch_for(b, smem);
+  e = launch_for(b, smem, mark);
   if (e != cudaSuccess) return e;
   return cudaMemcpyAsync(b->h_back, b->meta.p, kBackBytes, cudaMemcpyDeviceToHost, b->stream);
 }
@@ -440,14 +533,15 @@ int bxg_batch_create(bxg_batch* out, const bxg_config* cfg_in) {
     delete b;
     return BXG_ERR_CUDA;
   }
-  const int smem = int(kMaxTickScans * sizeof(TickScan));
-  // (29.7 KB is under the 48 KB default; the attribute is set for clarity)
-  cudaFuncSetAttribute(k_tick<32, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  cudaFuncSetAttribute(k_tick<16, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  cudaFuncSetAttribute(k_tick<8, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  cudaFuncSetAttribute(k_tick<32, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  cudaFuncSetAttribute(k_tick<16, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  cudaFuncSetAttribute(k_tick<8, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  const int smem = int(tick_smem(false));
+  cudaFuncSetAttribute(k_tick<32, 1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  cudaFuncSetAttribute(k_tick<16, 1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  cudaFuncSetAttribute(k_tick<8, 1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  cudaFuncSetAttribute(k_tick<32, 2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  cudaFuncSetAttribute(k_tick<16, 2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  cudaFuncSetAttribute(k_tick<8, 2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  cudaFuncSetAttribute(k_tick<32, 1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       int(tick_smem(true)));
   cudaGetLastError();
   const size_t pbytes = 256 + kMaxTickScans * sizeof(TickScan);
   if (cudaMallocHost(reinterpret_cast<void**>(&b->h_args), pbytes) != cudaSuccess ||
@@ -542,6 +636,8 @@ int bxg_batch_insert_f32(bxg_batch b, const bxg_pmap* maps, size_t n_scans, cons
   A.ctr_out = reinterpret_cast<uint32_t*>(meta + kOffCtr);
   A.times = reinterpret_cast<unsigned long long*>(meta + kOffTime);
   A.ray_prefix = reinterpret_cast<uint32_t*>(meta + kOffPrefix);
+  A.task_prefix = reinterpret_cast<uint32_t*>(meta + kOffTaskPrefix);
+  A.chunk = reinterpret_cast<uint32_t*>(meta + kOffChunk);
   A.n_scans = uint32_t(n_scans);
   A.total_points = total;
   A.total_tab = tab_total;
@@ -572,22 +668,36 @@ int bxg_batch_insert_f32(bxg_batch b, const bxg_pmap* maps, size_t n_scans, cons
     tb += tcap;
     S.keep_nonfinite = (pm->core.flags & BXG_FLAG_KEEP_NONFINITE) ? 1 : 0;
   }
+  // The two-phase ray update when every map can have its cube bitmap (each
+  // map's own buffers, zero between scans; growing them synchronises the map).
+  bool mark = true;
+  for (size_t s = 0; s < n_scans && mark; s++) {
+    TickScan& S = b->h_scans[s];
+    bool ok = false;
+    const int st = cube_for_scan(maps[s], S.ox, S.oy, S.oz, S.max_range, &S.Q, &ok);
+    if (st) return bfail(b, st, maps[s]->core.err);
+    mark = ok;
+  }
   b->back_bytes = kBackBytes;
   const size_t param_bytes = 256 + n_scans * sizeof(TickScan);
-  const size_t smem = kMaxTickScans * sizeof(TickScan);
+  const size_t smem = tick_smem(mark);
   if (!b->grid) {
     const bool u2 = b->ray_unroll == 2;
+    const size_t sm0 = tick_smem(false);
     switch (b->rays_per_warp) {
-      case 4: b->grid = u2 ? occupancy_grid<8, 2>(b, smem) : occupancy_grid<8, 1>(b, smem); break;
-      case 2: b->grid = u2 ? occupancy_grid<16, 2>(b, smem) : occupancy_grid<16, 1>(b, smem); break;
-      default: b->grid = u2 ? occupancy_grid<32, 2>(b, smem) : occupancy_grid<32, 1>(b, smem); break;
+      case 4: b->grid = u2 ? occupancy_grid<8, 2, false>(b, sm0) : occupancy_grid<8, 1, false>(b, sm0); break;
+      case 2: b->grid = u2 ? occupancy_grid<16, 2, false>(b, sm0) : occupancy_grid<16, 1, false>(b, sm0); break;
+      default: b->grid = u2 ? occupancy_grid<32, 2, false>(b, sm0) : occupancy_grid<32, 1, false>(b, sm0); break;
     }
-    if (b->grid <= 0) return bfail(b, BXG_ERR_CUDA, "k_tick cannot be resident");
+    b->grid_mark = occupancy_grid<32, 1, true>(b, tick_smem(true));
+    if (b->grid <= 0 || b->grid_mark <= 0)
+      return bfail(b, BXG_ERR_CUDA, "k_tick cannot be resident");
   }
 
   // Run: the captured graph when its shape matches, else capture it again.
-  const uint64_t key[6] = {uint64_t(b->params.p), param_bytes, uint64_t(b->meta.p), b->back_bytes,
-                           uint64_t(b->grid), b->rays_per_warp};
+  const uint64_t key[7] = {uint64_t(b->params.p), param_bytes, uint64_t(b->meta.p), b->back_bytes,
+                           uint64_t(mark ? b->grid_mark : b->grid), b->rays_per_warp,
+                           mark ? 1ull : 0ull};
   cudaEventRecord(b->ev0, b->stream);
   bool ran = false;
   if (b->use_graph) {
@@ -598,7 +708,7 @@ int bxg_batch_insert_f32(bxg_batch b, const bxg_pmap* maps, size_t n_scans, cons
       b->graph = nullptr;
       b->graph_ok = false;
       if (cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
-        const cudaError_t e1 = enqueue_tick(b, param_bytes, smem);
+        const cudaError_t e1 = enqueue_tick(b, param_bytes, smem, mark);
         const cudaError_t e2 = cudaStreamEndCapture(b->stream, &b->graph);
         if (e1 == cudaSuccess && e2 == cudaSuccess &&
             cudaGraphInstantiate(&b->exec, b->graph, 0) == cudaSuccess) {
@@ -613,7 +723,7 @@ int bxg_batch_insert_f32(bxg_batch b, const bxg_pmap* maps, size_t n_scans, cons
       ran = true;
     }
   }
-  if (!ran) BB_CUDA(b, enqueue_tick(b, param_bytes, smem));
+  if (!ran) BB_CUDA(b, enqueue_tick(b, param_bytes, smem, mark));
   cudaEventRecord(b->ev1, b->stream);
   BB_CUDA(b, cudaStreamSynchronize(b->stream));
   b->launches++;
@@ -680,7 +790,7 @@ int bxg_batch_stats(bxg_batch b, double out[8]) {
   out[1] = b->graph_ok ? 1 : 0;
   out[2] = double(b->last_retries);
   out[3] = double(b->ticks);
-  out[4] = double(b->grid);
+  out[4] = double(b->grid_mark ? b->grid_mark : b->grid);
   out[5] = double(b->launches);
   out[6] = b->phase_ms[1];  // endpoints
   out[7] = b->phase_ms[2] + b->phase_ms[4];  // winners + rays

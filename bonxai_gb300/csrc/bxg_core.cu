@@ -330,12 +330,38 @@ int core_init(MapCore* m, double res, int ib, int lb, size_t esz, const bxg_conf
   BXG_CUDA(m, cudaMemsetAsync(m->buckets.p, 0xFF, size_t(hp) * 16, m->stream));
   d.buckets = m->buckets.as<uint4>();
   d.hmask = hp - 1;
-  int st = grow_inner(m, cfg.initial_inners ? cfg.initial_inners : 1024);
+  m->init_inners = cfg.initial_inners ? cfg.initial_inners : 1024;
+  m->init_leaves = cfg.initial_leaves ? cfg.initial_leaves : 4096;
+  int st = grow_inner(m, m->init_inners);
   if (st) return st;
-  st = grow_leaf(m, cfg.initial_leaves ? cfg.initial_leaves : 4096);
+  st = grow_leaf(m, m->init_leaves);
   if (st) return st;
   BXG_CUDA(m, cudaStreamSynchronize(m->stream));
   return BXG_OK;
+}
+
+int core_release_pools(MapCore* m) {
+  BXG_CUDA(m, cudaStreamSynchronize(m->stream));
+  m->leaf_gen++;
+  m->ichild.release();
+  m->imask.release();
+  m->lmask.release();
+  m->ldata.release();
+  m->lkey.release();
+  m->lfree.release();
+  m->dm.icap = m->dm.lcap = 0;
+  m->dm.ichild = nullptr;
+  m->dm.imask = nullptr;
+  m->dm.lmask = nullptr;
+  m->dm.ldata = nullptr;
+  m->dm.lkey = nullptr;
+  m->dm.lfree = nullptr;
+  m->dm.has_free = 0;
+  int st = grow_inner(m, m->init_inners);
+  if (st) return st;
+  st = grow_leaf(m, m->init_leaves);
+  if (st) return st;
+  return core_clear(m);
 }
 
 int core_clear(MapCore* m) {

@@ -60,6 +60,8 @@ enum : int {
   C_ERR = 3,        // error bits
   C_CAST = 4,       // rays queued for the current scan
   C_FREE_LEAF = 5,  // entries on the leaf free stack
+  C_LIST = 6,       // leaf blocks on the scan's marked list (bxg_mark.cuh)
+  C_TASK = 7,       // next block task of the mark phase
   C_STATS = 8,      // 64-bit statistics start here (pairs of words)
   C_WORDS = 32,
 };

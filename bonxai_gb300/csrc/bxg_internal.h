@@ -72,6 +72,7 @@ struct MapCore {
   double res = 0, inv_res = 0;
   DMap dm{};
   size_t budget = 0;
+  size_t init_inners = 0, init_leaves = 0;  // pool sizes at creation
   float load_factor = 0.5f;
   uint32_t rays_per_warp = 0, block_size = 0, ray_unroll = 0;
   // bumped whenever leaf slots may be released (clear, releaseUnusedMemory):
@@ -113,6 +114,9 @@ int cuda_fail(MapCore* m, cudaError_t e, const char* what);
 // Lifecycle and pools (bxg_core.cu).
 int core_init(MapCore* m, double res, int ib, int lb, size_t esz, const bxg_config* cfg);
 int core_clear(MapCore* m);
+// clear(CLEAR_MEMORY) that also gives the node pools' memory back: the pools
+// shrink to their sizes at creation (bonxai.hpp:678-684).
+int core_release_pools(MapCore* m);
 // Reads the counters back (synchronising the stream) and converts device error
 // bits into a status; clears them and repairs overshooting allocation counters.
 int core_sync(MapCore* m, uint32_t* err_bits_out = nullptr);
@@ -180,6 +184,10 @@ struct bxg_pmap_s {
   uint32_t dir_epoch = 0;
   uint64_t dir_gen = 0;
   bool dir_live = false;
+  // the ray phase's cube bitmap, list bits and list (bxg_mark.cuh): all zero
+  // between scans; sized for cube_blocks leaf blocks
+  bxg::DevBuf cube_bits, cube_touch, cube_list;
+  size_t cube_blocks = 0;
   cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   ~bxg_pmap_s() {
     for (auto& e : ev)
@@ -189,6 +197,12 @@ struct bxg_pmap_s {
 
 namespace bxg {
 struct LeafDir;
+struct RayCube;
+// The cube bitmap of a scan's ray phase from origin cell (ox, oy, oz) whose
+// rays end within `reach` (world units) of the origin: *ok = false when the
+// scan cannot use one (leaf_bits other than 3, non-finite points kept, a cube
+// above the size limit); buffers grow here (cudaMalloc, zeroed).
+int cube_for_scan(bxg_pmap_s* pm, int ox, int oy, int oz, double reach, RayCube* Q, bool* ok);
 // Sets up the ray walk's leaf directory of a scan (bxg_pmap.cu).
 // Memsets (first use, epoch wrap) go to `stream` (nullptr: the map's own).
 int leaf_dir_for_scan(bxg_pmap_s* pm, int ox, int oy, int oz, LeafDir* D, size_t max_words,

@@ -13,15 +13,22 @@
 //                 {cell, hit/miss} to the ray list (and counts the ray length
 //                 for the ray-cell total).
 //   k_apply       only after a pool ran out: completes the listed endpoints.
-//   k_rays        lane-strided Bresenham over every listed ray: a group of W
-//                 lanes walks one ray, W consecutive cells per step, creating
-//                 leaves on the way and applying the miss update.
+//   k_mark        the ray phase's first half: every listed ray's cells set
+//                 their bits in the scan's cube bitmap (bxg_mark.cuh).
+//   k_apply_rays  its second half: per marked leaf, get-or-create the leaf and
+//                 apply the miss update to its marked cells.
+//   k_rays        the single-pass form of the ray phase, for scans the cube
+//                 does not cover (rays queued by addHitPoint/addMissPoint,
+//                 kept non-finite points, cubes above the size limit): a group
+//                 of W lanes walks one ray, W consecutive cells per step,
+//                 creating leaves on the way and applying the miss update.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
 
 #include "bxg_internal.h"
+#include "bxg_mark.cuh"
 #include "bxg_scan.cuh"
 
 namespace bxg {
@@ -230,6 +237,57 @@ __global__ void __launch_bounds__(U == 2 ? 256 : 1024, U == 2 ? 3 : 1) k_rays(DM
   }
 }
 
+// Mark phase: block tasks of consecutive rays of the list (taken from the
+// counter *task, zero at launch), marked by mark_rays_block. Also clears
+// tab[0, tab_n), the scan's endpoint dedup table, for the next scan.
+__global__ void __launch_bounds__(1024) k_mark(DMap M, RayCube Q, const int4* __restrict__ cast,
+                                               uint32_t cast_cap, int ox, int oy, int oz,
+                                               uint4* __restrict__ tab, uint32_t tab_n,
+                                               uint32_t* task) {
+  __shared__ uint32_t sm[kMarkSmemWords];
+  __shared__ uint32_t s_next, s_task;
+  for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < tab_n; t += gridDim.x * blockDim.x)
+    tab[t] = make_uint4(kNone, kNone, kNone, kNone);
+  for (int t = threadIdx.x; t < kMarkSmemWords; t += blockDim.x) sm[t] = 0u;
+  const uint32_t n_cast = min(ld_volatile(M.ctr + C_CAST), cast_cap);
+  // about four tasks per block, at least 64 rays each
+  const uint32_t chunk = max(64u, (n_cast + 4u * gridDim.x - 1) / (4u * gridDim.x));
+  const uint32_t n_tasks = (n_cast + chunk - 1) / chunk;
+  uint32_t visited = 0;
+  for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0) s_task = atomicAdd(task, 1u);
+    __syncthreads();
+    const uint32_t t = s_task;
+    if (t >= n_tasks) break;
+    const uint32_t r0 = t * chunk;
+    mark_rays_block<kMarkNB>(M, Q, cast, r0, min(n_cast, r0 + chunk), ox, oy, oz, sm, &s_next,
+                             visited);
+  }
+  visited = __reduce_add_sync(0xffffffffu, visited);
+  if ((threadIdx.x & 31) == 0 && visited)
+    atomicAdd(reinterpret_cast<unsigned long long*>(M.ctr + C_STATS) + S_VISITED,
+              static_cast<unsigned long long>(visited));
+}
+
+// Apply phase: a group of kApplyGroup lanes per listed leaf block.
+__global__ void __launch_bounds__(256) k_apply_rays(DMap M, RayCube Q, int32_t u, int32_t miss,
+                                                    int32_t cmin) {
+  const uint32_t n = min(ld_volatile(Q.count), Q.cap);
+  const unsigned lane = threadIdx.x & 31;
+  const unsigned sl = lane & (kApplyGroup - 1), gbase = lane & ~unsigned(kApplyGroup - 1);
+  const unsigned gmask = ((1u << kApplyGroup) - 1u) << gbase;
+  const uint32_t gid = (blockIdx.x * blockDim.x + threadIdx.x) / kApplyGroup;
+  const uint32_t ng = (gridDim.x * blockDim.x) / kApplyGroup;
+  uint32_t updated = 0;
+  for (uint32_t i = gid; i < n; i += ng)
+    apply_block(M, Q, Q.list[i], u, miss, cmin, sl, gbase, gmask, updated);
+  updated = __reduce_add_sync(0xffffffffu, updated);
+  if (lane == 0 && updated)
+    atomicAdd(reinterpret_cast<unsigned long long*>(M.ctr + C_STATS) + S_UPDATED,
+              static_cast<unsigned long long>(updated));
+}
+
 // isOccupied / isUnknown / isFree (probabilistic_map.cpp:56-75).
 __global__ void k_query(DMap M, const int32_t* __restrict__ xyz, uint32_t n, int mode,
                         int32_t thr, uint8_t* __restrict__ out) {
@@ -421,6 +479,51 @@ int leaf_dir_for_scan(bxg_pmap_s* pm, int ox, int oy, int oz, LeafDir* D, size_t
 }
 }  // namespace bxg
 
+namespace bxg {
+// Largest cube side (leaves): 200^3 blocks of 64 B = 512 MB of bits. Scans
+// whose cube would be larger (very fine resolutions with long ranges) walk
+// their rays with k_rays instead.
+constexpr uint32_t kMaxCubeSide = 200;
+
+int cube_for_scan(bxg_pmap_s* pm, int ox, int oy, int oz, double reach, RayCube* Q, bool* ok) {
+  MapCore* m = &pm->core;
+  *ok = false;
+  if (m->dm.lb != 3 || m->dm.esz != 4 || (m->flags & BXG_FLAG_KEEP_NONFINITE)) return BXG_OK;
+  if (!(reach > 0) || !std::isfinite(reach)) return BXG_OK;
+  // Ray ends lie within ceil(reach / res) + 2 cells of the origin cell (the
+  // floor of the origin and of the end each move a cell by less than one), so
+  // every ray cell lies within HL leaves of the origin's leaf.
+  const double cells = std::ceil(reach * m->inv_res) + 2.0;
+  if (!(cells < 8.0 * kMaxCubeSide)) return BXG_OK;
+  const int R = int(cells);
+  const int HL = std::max((R + 7) / 8 + 1, kMarkNB + 1);
+  const uint32_t S = uint32_t(2 * HL + 1);
+  if (S > kMaxCubeSide) return BXG_OK;
+  const size_t blocks = size_t(S) * S * S;
+  if (blocks > pm->cube_blocks) {
+    BXG_CUDA(m, pm->cube_bits.ensure(blocks * 64));
+    BXG_CUDA(m, pm->cube_touch.ensure(((blocks + 31) / 32) * 4));
+    BXG_CUDA(m, pm->cube_list.ensure(blocks * 4));
+    BXG_CUDA(m, cudaMemsetAsync(pm->cube_bits.p, 0, pm->cube_bits.cap, m->stream));
+    BXG_CUDA(m, cudaMemsetAsync(pm->cube_touch.p, 0, pm->cube_touch.cap, m->stream));
+    // the batched tick uses the buffers from another stream
+    BXG_CUDA(m, cudaStreamSynchronize(m->stream));
+    pm->cube_blocks = blocks;
+  }
+  Q->bits = pm->cube_bits.as<uint32_t>();
+  Q->touched = pm->cube_touch.as<uint32_t>();
+  Q->list = pm->cube_list.as<uint32_t>();
+  Q->count = m->ctr.as<uint32_t>() + C_LIST;
+  Q->x0 = ((ox >> 3) - HL) * 8;
+  Q->y0 = ((oy >> 3) - HL) * 8;
+  Q->z0 = ((oz >> 3) - HL) * 8;
+  Q->S = S;
+  Q->cap = uint32_t(blocks);
+  *ok = true;
+  return BXG_OK;
+}
+}  // namespace bxg
+
 namespace {
 
 using RayKernel = void (*)(DMap, const int4*, uint32_t, int, int, int, int32_t, int32_t, int32_t,
@@ -442,6 +545,35 @@ RayKernel ray_kernel(uint32_t rpw, bool u2) {
 // U = 2 kernels hold 80 registers and launch 256 threads.
 int launch_rays(bxg_pmap_s* pm, int ox, int oy, int oz) {
   MapCore* m = &pm->core;
+  if (!pm->cast_ub) return BXG_OK;
+  {
+    // two-phase form: mark the rays' cells, then apply per leaf
+    RayCube Q{};
+    bool ok = false;
+    int st = cube_for_scan(pm, ox, oy, oz, pm->dir_reach, &Q, &ok);
+    if (st) return st;
+    if (ok) {
+      const Opts o = opts_of(pm);
+      const uint32_t ccap = uint32_t(m->s_cast.cap / 16);
+      const uint32_t tab_n = m->dedup_used;
+      BXG_CUDA(m, cudaMemsetAsync(m->ctr.as<uint32_t>() + C_LIST, 0, 8, m->stream));
+      const unsigned mblocks =
+          unsigned(std::min<uint64_t>(m->sm_count, std::max<uint64_t>(1, pm->cast_ub / 256)));
+      k_mark<<<mblocks, 1024, 0, m->stream>>>(m->dm, Q, m->s_cast.as<int4>(), ccap, ox, oy, oz,
+                                             m->s_dedup.as<uint4>(), tab_n,
+                                             m->ctr.as<uint32_t>() + C_TASK);
+      BXG_LAUNCHED(m);
+      // 16 groups per 256-thread block; the list holds at most min(cube, 64 x rays) blocks
+      const uint64_t groups = std::min<uint64_t>(Q.cap, pm->cast_ub * 64);
+      const unsigned ablocks = unsigned(std::min<uint64_t>(uint64_t(m->sm_count) * 8,
+                                                           std::max<uint64_t>(1, (groups + 15) / 16)));
+      k_apply_rays<<<ablocks, 256, 0, m->stream>>>(m->dm, Q, pm->update_count, o.miss, o.cmin);
+      BXG_LAUNCHED(m);
+      m->dedup_clean = std::max(m->dedup_clean, tab_n);
+      m->dedup_used = 0;
+      return BXG_OK;
+    }
+  }
   const uint32_t rpw = m->rays_per_warp ? m->rays_per_warp : 1;
   const bool u2 = m->ray_unroll == 2;
   const int bs_max = u2 ? 256 : 1024;
@@ -527,6 +659,7 @@ int finish_scan(bxg_pmap_s* pm, int ox, int oy, int oz, bool cast_rays, uint64_t
     // end of scan: empty the ray list (the next scan's first kernel zeroes
     // the device count), advance the counter (cpp:301-310)
     pm->cast_ub = 0;
+    pm->dir_reach = 0.0;
     if (++pm->update_count == 4) pm->update_count = 1;
   }
   return core_maintain(m);
@@ -646,6 +779,8 @@ int add_points(bxg_pmap m_, const double* xyz, size_t n, int kind,
   if (!xyz || n >= 0x7FFFFFFFu) return set_error(m, BXG_ERR_INVALID_ARG, "null input");
   cudaSetDevice(m->device);
   record(pm, 0);
+  // rays queued here may end anywhere: the coming ray phase has no bound
+  pm->dir_reach = 0.0;
   // the first batch after a scan starts the statistics and the ray list
   const int zero = pm->cast_ub == 0 ? (ZERO_STATS | ZERO_CAST) : 0;
   const void* dpts = nullptr;

@@ -12,9 +12,15 @@
 // so every request sees exactly the map state it would see alone. All maps'
 // "before" lookups run as one kernel, all inserts as one batched tick
 // (bxg_batch.cu), all "after" lookups as one kernel: the work of different
-// clients overlaps on the device. Admission: insert slots per tick, points per
-// tick, and an HBM budget across all maps' node pools (an insert that would
-// need more is rejected with BXG_ERR_OUT_OF_POOL).
+// clients overlaps on the device. A clear request (clear(CLEAR_MEMORY),
+// bonxai.hpp:678-684, which can also give the map's pool memory back) takes an
+// insert's place in its map's tick and runs before the inserts.
+// Admission: insert slots per tick, points per tick, and an HBM budget across
+// all maps' node pools. An insert that does not fit the budget stays at the
+// head of its map's queue (with the requests behind it) until memory frees up
+// -- another map's clear -- and is admitted then; only when it has waited
+// past the server's admission timeout does it complete with
+// BXG_ERR_OUT_OF_POOL.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -76,7 +82,7 @@ using namespace bxg;
 using Clock = std::chrono::steady_clock;
 
 namespace {
-enum Kind : int { K_INSERT = 0, K_QUERY = 1, K_OCCUPIED = 2 };
+enum Kind : int { K_INSERT = 0, K_QUERY = 1, K_OCCUPIED = 2, K_CLEAR = 3 };
 
 struct Request {
   uint64_t ticket = 0;
@@ -95,6 +101,7 @@ struct Request {
   std::vector<uint8_t> answers;
   std::vector<int32_t> occupied;
   Clock::time_point t_submit, t_start, t_done;
+  Clock::time_point deadline;  // inserts: admission gives up after this
   uint64_t tick = 0;
 };
 }  // namespace
@@ -108,6 +115,7 @@ struct bxg_server_s {
   uint32_t max_scans = 128;
   uint64_t max_points = 64ull << 20;
   uint64_t max_lookups = 64ull << 20;
+  double admission_timeout_s = 10.0;
   // queues
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
@@ -116,6 +124,7 @@ struct bxg_server_s {
   uint64_t next_ticket = 1;
   size_t queued = 0, in_flight = 0;
   bool stop = false;
+  bool kick = false;  // a submission arrived (wakes a worker waiting on deferred inserts)
   std::thread worker;
   // staging
   DevBuf d_pts, d_xyz, d_ans, d_desc;
@@ -125,6 +134,7 @@ struct bxg_server_s {
   // statistics
   std::vector<double> lat_all, lat_ins, lat_q, lat_occ;
   uint64_t completed = 0, n_ins = 0, n_q = 0, n_occ = 0, ticks = 0, rejected = 0;
+  uint64_t deferred = 0;  // insert admissions postponed for lack of budget
   uint64_t ray_cells = 0, lookups = 0;
   double busy_s = 0;
   size_t pool_bytes = 0;  // all maps' pools, refreshed by the worker after each tick
@@ -230,70 +240,119 @@ size_t pools_bytes(bxg_server_s* s) {
   return b;
 }
 
+// Bytes an insert of n points may add to its map's pools (the leaf headroom
+// the batched tick reserves).
+size_t insert_need(size_t n) { return (n / 4 + 1024) * (64 + 2048 + 20); }
+
 void worker_loop(bxg_server_s* s) {
   cudaSetDevice(s->device);
-  uint32_t rr = 0;  // round-robin start for fairness
+  uint32_t rr = 0;         // round-robin start for fairness
+  bool idle_wait = false;  // the last tick could only defer inserts
+  Clock::time_point wake{};
+  // a map's part of a tick: lookups (in `before`), then one insert or clear,
+  // then the lookups behind it
+  struct MapTick {
+    uint32_t map = 0;
+    Request* mid = nullptr;
+    std::vector<Request*> after;
+  };
   for (;;) {
-    std::vector<Request*> before, inserts, after;
+    std::vector<Request*> before;
+    std::vector<MapTick> mids;
     {
       std::unique_lock<std::mutex> lk(s->mu);
-      s->cv_work.wait(lk, [&] { return s->stop || s->queued > 0; });
+      if (idle_wait)
+        s->cv_work.wait_until(lk, wake, [&] { return s->stop || s->kick; });
+      else
+        s->cv_work.wait(lk, [&] { return s->stop || s->queued > 0; });
+      s->kick = false;
       if (s->stop && s->queued == 0) return;
       uint64_t pts = 0, looks = 0;
+      uint32_t n_ins = 0;
       const uint32_t nm = uint32_t(s->maps.size());
+      auto is_mid = [](const Request* r) { return r->kind == K_INSERT || r->kind == K_CLEAR; };
       for (uint32_t j = 0; j < nm; j++) {
         const uint32_t m = (rr + j) % nm;
         auto& q = s->fifo[m];
-        while (!q.empty() && q.front()->kind != K_INSERT && looks < s->max_lookups) {
+        while (!q.empty() && !is_mid(q.front()) && looks < s->max_lookups) {
           looks += q.front()->coords.size() / 3;
           before.push_back(q.front());
           q.pop_front();
         }
-        if (!q.empty() && q.front()->kind == K_INSERT && inserts.size() < s->max_scans &&
-            (inserts.empty() || pts + q.front()->pts.size() / 3 <= s->max_points)) {
-          pts += q.front()->pts.size() / 3;
-          inserts.push_back(q.front());
-          q.pop_front();
-          while (!q.empty() && q.front()->kind != K_INSERT && looks < s->max_lookups) {
-            looks += q.front()->coords.size() / 3;
-            after.push_back(q.front());
-            q.pop_front();
-          }
+        if (q.empty() || !is_mid(q.front())) continue;
+        Request* r = q.front();
+        if (r->kind == K_INSERT) {
+          if (n_ins >= s->max_scans || (n_ins && pts + r->pts.size() / 3 > s->max_points))
+            continue;
+          pts += r->pts.size() / 3;
+          n_ins++;
         }
+        q.pop_front();
+        MapTick mt;
+        mt.map = m;
+        mt.mid = r;
+        while (!q.empty() && !is_mid(q.front()) && looks < s->max_lookups) {
+          looks += q.front()->coords.size() / 3;
+          mt.after.push_back(q.front());
+          q.pop_front();
+        }
+        mids.push_back(std::move(mt));
       }
       rr = (rr + 1) % std::max<uint32_t>(nm, 1);
-      const size_t taken = before.size() + inserts.size() + after.size();
+      size_t taken = before.size();
+      for (auto& mt : mids) taken += 1 + mt.after.size();
       s->queued -= taken;
       s->in_flight += taken;
     }
     const Clock::time_point t0 = Clock::now();
-    for (auto* v : {&before, &inserts, &after})
-      for (Request* r : *v) r->t_start = t0;
+    for (Request* r : before) r->t_start = t0;
 
     int st = run_lookups(s, before);
     if (st)
       for (Request* r : before) r->status = st;
 
-    // admission against the HBM budget, then one batched tick
-    std::vector<Request*> admit;
+    // clears first: they can free pool memory for this tick's inserts
+    for (auto& mt : mids) {
+      if (mt.mid->kind != K_CLEAR) continue;
+      bxg_pmap m = s->maps[mt.map];
+      m->cast_ub = 0;
+      mt.mid->status = mt.mid->mode ? core_release_pools(&m->core) : core_clear(&m->core);
+      mt.mid->t_start = t0;
+    }
+    // admission against the HBM budget; an insert that does not fit waits
+    // (it and the requests behind it go back to the head of its queue) until
+    // its deadline
+    std::vector<MapTick*> admit;
+    std::vector<MapTick> deferred;
     size_t used = pools_bytes(s);
-    for (Request* r : inserts) {
-      const size_t n = r->pts.size() / 3;
-      const size_t need = (n / 4 + 1024) * (64 + 2048 + 20);  // leaf headroom the tick reserves
-      if (used + need > s->budget) {
+    for (auto& mt : mids) {
+      Request* r = mt.mid;
+      if (r->kind != K_INSERT) continue;
+      const size_t need = insert_need(r->pts.size() / 3);
+      if (used + need <= s->budget) {
+        used += need;
+        r->t_start = t0;
+        admit.push_back(&mt);
+      } else if (t0 >= r->deadline) {
         r->status = BXG_ERR_OUT_OF_POOL;
+        r->t_start = t0;
         s->rejected++;
-        continue;
+      } else {
+        MapTick d;
+        d.map = mt.map;
+        d.mid = r;
+        d.after.swap(mt.after);
+        deferred.push_back(std::move(d));
+        mt.mid = nullptr;
       }
-      used += need;
-      admit.push_back(r);
     }
     if (!admit.empty()) {
       std::vector<bxg_pmap> ms;
       std::vector<uint64_t> off(1, 0);
       std::vector<float> org;
       std::vector<double> mr;
-      for (Request* r : admit) {
+      for (MapTick* mt : admit) {
+        Request* r = mt->mid;
         ms.push_back(s->maps[r->map]);
         off.push_back(off.back() + r->pts.size() / 3);
         org.insert(org.end(), r->origin, r->origin + 3);
@@ -301,53 +360,88 @@ void worker_loop(bxg_server_s* s) {
       }
       s->h_pts.resize(3 * off.back());
       for (size_t k = 0; k < admit.size(); k++)
-        std::memcpy(s->h_pts.data() + 3 * off[k], admit[k]->pts.data(), admit[k]->pts.size() * 4);
+        std::memcpy(s->h_pts.data() + 3 * off[k], admit[k]->mid->pts.data(),
+                    admit[k]->mid->pts.size() * 4);
       std::vector<uint64_t> rc(admit.size(), 0);
       st = bxg_batch_insert_f32(s->batch, ms.data(), ms.size(), s->h_pts.data(), off.data(),
                                 org.data(), mr.data(), rc.data());
       for (size_t k = 0; k < admit.size(); k++) {
-        admit[k]->status = st;
-        admit[k]->ray_cells = rc[k];
+        admit[k]->mid->status = st;
+        admit[k]->mid->ray_cells = rc[k];
         s->ray_cells += rc[k];
       }
       if (st) s->err = bxg_batch_last_error(s->batch);
     }
 
+    std::vector<Request*> after;
+    for (auto& mt : mids)
+      if (mt.mid)
+        for (Request* r : mt.after) {
+          r->t_start = t0;
+          after.push_back(r);
+        }
     st = run_lookups(s, after);
     if (st)
       for (Request* r : after) r->status = st;
 
     const Clock::time_point t1 = Clock::now();
     const size_t pb = pools_bytes(s);
+    size_t done_n = before.size() + after.size();
+    for (auto& mt : mids)
+      if (mt.mid) done_n++;
     {
       std::lock_guard<std::mutex> lk(s->mu);
       s->pool_bytes = pb;
       s->busy_s += std::chrono::duration<double>(t1 - t0).count();
-      s->ticks++;
-      for (auto* v : {&before, &inserts, &after}) {
-        for (Request* r : *v) {
-          r->t_done = t1;
-          r->done = true;
-          r->tick = s->ticks;
-          const double lat = ms_between(r->t_submit, r->t_done);
-          s->lat_all.push_back(lat);
-          (r->kind == K_INSERT ? s->lat_ins : r->kind == K_QUERY ? s->lat_q : s->lat_occ)
-              .push_back(lat);
-          (r->kind == K_INSERT ? s->n_ins : r->kind == K_QUERY ? s->n_q : s->n_occ)++;
-          s->completed++;
-          s->t_last = t1;
-          if (r->discard) {
-            s->live.erase(r->ticket);
-            delete r;
-          } else {
-            r->pts.clear();
-            r->pts.shrink_to_fit();
-            r->coords.clear();
-            r->coords.shrink_to_fit();
-          }
+      if (done_n) s->ticks++;
+      auto finish = [&](Request* r) {
+        r->t_done = t1;
+        r->done = true;
+        r->tick = s->ticks;
+        const double lat = ms_between(r->t_submit, r->t_done);
+        s->lat_all.push_back(lat);
+        if (r->kind == K_INSERT) {
+          s->lat_ins.push_back(lat);
+          s->n_ins++;
+        } else if (r->kind == K_QUERY) {
+          s->lat_q.push_back(lat);
+          s->n_q++;
+        } else if (r->kind == K_OCCUPIED) {
+          s->lat_occ.push_back(lat);
+          s->n_occ++;
         }
+        s->completed++;
+        s->t_last = t1;
+        if (r->discard) {
+          s->live.erase(r->ticket);
+          delete r;
+        } else {
+          r->pts.clear();
+          r->pts.shrink_to_fit();
+          r->coords.clear();
+          r->coords.shrink_to_fit();
+        }
+      };
+      for (Request* r : before) finish(r);
+      for (auto& mt : mids)
+        if (mt.mid) finish(mt.mid);
+      for (Request* r : after) finish(r);
+      // deferred inserts and the lookups behind them go back, in order
+      Clock::time_point first_deadline = Clock::time_point::max();
+      for (auto& d : deferred) {
+        auto& q = s->fifo[d.map];
+        for (auto it = d.after.rbegin(); it != d.after.rend(); ++it) q.push_front(*it);
+        q.push_front(d.mid);
+        first_deadline = std::min(first_deadline, d.mid->deadline);
+        s->queued += 1 + d.after.size();
+        s->in_flight -= 1 + d.after.size();
+        s->deferred++;
       }
-      s->in_flight -= before.size() + inserts.size() + after.size();
+      s->in_flight -= done_n;
+      // only deferred inserts are left: sleep until a submission or the next
+      // check (every 50 ms at most, so that a deadline is noticed)
+      idle_wait = done_n == 0 && !deferred.empty();
+      if (idle_wait) wake = std::min(first_deadline, t1 + std::chrono::milliseconds(50));
     }
     s->cv_done.notify_all();
   }
@@ -378,9 +472,13 @@ int submit(bxg_server_s* s, Request* r, uint64_t* ticket) {
       s->t_first = r->t_submit;
       s->have_first = true;
     }
+    if (r->kind == K_INSERT)
+      r->deadline = r->t_submit + std::chrono::duration_cast<Clock::duration>(
+                                      std::chrono::duration<double>(s->admission_timeout_s));
     s->live[r->ticket] = r;
     s->fifo[r->map].push_back(r);
     s->queued++;
+    s->kick = true;
     if (ticket) *ticket = r->ticket;
   }
   s->cv_work.notify_one();
@@ -411,6 +509,7 @@ int bxg_server_create(bxg_server* out, const double* resolutions, size_t n_maps,
   s->max_scans = cfg.max_scans_per_tick ? std::min<uint32_t>(cfg.max_scans_per_tick, 128) : 128;
   if (cfg.max_points_per_tick) s->max_points = cfg.max_points_per_tick;
   if (cfg.max_lookups_per_tick) s->max_lookups = cfg.max_lookups_per_tick;
+  if (cfg.admission_timeout_s > 0) s->admission_timeout_s = cfg.admission_timeout_s;
   bxg_config mc;
   bxg_config_default(&mc);
   mc.device = s->device;
@@ -479,6 +578,17 @@ int bxg_server_query(bxg_server s, uint32_t map, const int32_t* xyz, size_t n, i
   return submit(s, r, ticket);
 }
 
+int bxg_server_clear(bxg_server s, uint32_t map, int release_memory, int discard,
+                     uint64_t* ticket) {
+  if (!s) return BXG_ERR_INVALID_ARG;
+  Request* r = new Request();
+  r->kind = K_CLEAR;
+  r->map = map;
+  r->mode = release_memory ? 1 : 0;
+  r->discard = discard != 0;
+  return submit(s, r, ticket);
+}
+
 int bxg_server_get_occupied(bxg_server s, uint32_t map, int discard, uint64_t* ticket) {
   if (!s) return BXG_ERR_INVALID_ARG;
   Request* r = new Request();
@@ -520,7 +630,7 @@ int bxg_server_wait(bxg_server s, uint64_t ticket, double timeout_s, bxg_server_
   }
   // A call without an output buffer only reports the result size and keeps
   // the ticket, so that the caller can size a buffer and call again.
-  if (out || r->kind == K_INSERT) {
+  if (out || r->kind == K_INSERT || r->kind == K_CLEAR) {
     s->live.erase(it);
     delete r;
   }
@@ -557,7 +667,7 @@ int bxg_server_stats(bxg_server s, double out[20]) {
   out[16] = pct(s->lat_occ, 0.5);
   out[17] = pct(s->lat_occ, 0.99);
   out[18] = double(s->pool_bytes);
-  out[19] = 0;
+  out[19] = double(s->deferred);
   return BXG_OK;
 }
 

@@ -366,7 +366,10 @@ int bxg_batch_phase_ms(bxg_batch b, double out[5]);
  * (probabilistic_map.hpp:91-124). A worker thread batches whatever is queued
  * into ticks (continuous batching); requests on one map run in submission
  * order and see exactly the state they would see alone. Admission: insert
- * slots and points per tick, and an HBM budget across all maps' node pools.
+ * slots and points per tick, and an HBM budget across all maps' node pools;
+ * an insert that does not fit the budget waits at the head of its map's queue
+ * until memory frees up (a clear of another map), and completes with
+ * BXG_ERR_OUT_OF_POOL only after admission_timeout_s.
  * ======================================================================== */
 typedef struct bxg_server_s* bxg_server;
 
@@ -380,11 +383,12 @@ typedef struct {
   uint32_t ray_unroll;           /* batched ray kernel, 1/2 */
   uint32_t flags;                /* BXG_FLAG_* for the maps and the batch */
   uint32_t initial_leaves;       /* per map; 0 = 4096 */
+  double admission_timeout_s;    /* an insert waits this long for budget; 0 = 10 s */
 } bxg_server_config;
 
 typedef struct {
   int status;        /* bxg_status of the request */
-  int kind;          /* 0 insert, 1 lookup, 2 getOccupiedVoxels */
+  int kind;          /* 0 insert, 1 lookup, 2 getOccupiedVoxels, 3 clear */
   uint32_t map;
   uint64_t ray_cells;/* inserts: ray-cell updates */
   size_t n_out;      /* lookups: answers; getOccupiedVoxels: coordinates */
@@ -409,6 +413,12 @@ int bxg_server_insert(bxg_server s, uint32_t map, const float* xyz, size_t n,
 int bxg_server_query(bxg_server s, uint32_t map, const int32_t* xyz, size_t n, int mode,
                      int discard, uint64_t* ticket);
 int bxg_server_get_occupied(bxg_server s, uint32_t map, int discard, uint64_t* ticket);
+/* clear(CLEAR_MEMORY) of a map (bonxai_core/include/bonxai/bonxai.hpp:678-684)
+ * in its request order; with release_memory the map's node pools shrink back
+ * to their sizes at creation, which frees budget for waiting inserts. The
+ * result's kind is 3. */
+int bxg_server_clear(bxg_server s, uint32_t map, int release_memory, int discard,
+                     uint64_t* ticket);
 /* Waits for a ticket; copies lookup answers (cap bytes) or occupied
  * coordinates (cap coordinates) to out and releases the ticket. With
  * out == NULL a lookup or getOccupiedVoxels ticket is kept: res->n_out tells
@@ -421,7 +431,7 @@ int bxg_server_drain(bxg_server s, double timeout_s);
  * [6] p99 ms [7] insert p50 [8] insert p99 [9] lookup p50 [10] lookup p99
  * [11] ray-cell updates [12] lookup coordinates [13] rejected [14] busy s
  * [15] first submission to last completion s [16] occupied p50 [17] occupied
- * p99 [18] pool bytes of all maps [19] reserved. */
+ * p99 [18] pool bytes of all maps [19] insert admissions postponed for budget. */
 int bxg_server_stats(bxg_server s, double out[20]);
 /* The map of one client (for inspection after bxg_server_drain). */
 bxg_pmap bxg_server_map(bxg_server s, uint32_t map);

@@ -420,3 +420,38 @@ def test_queries_on_cells_with_zero_words(gpu):
     assert np.array_equal(m.is_occupied(q), want_occ)
     assert np.array_equal(m.is_unknown(q), want_unk)
     assert np.array_equal(m.is_free(q), want_fre)
+
+
+def test_ray_phase_counts_each_updated_cell_once(gpu):
+    """The two-phase ray update (mark the ray cells, then apply per leaf)
+    updates each cell once, so its counter is the exact number of cells the
+    ray phase changed: cells whose update_id became the scan's counter, minus
+    the endpoint cells (one per cast ray)."""
+    scene = synth.LidarScene()
+    m = gpu.ProbabilisticMap(0.1)
+    for k in range(5):
+        pts, org = scene.scan(k, n_points=40000)
+        u = m.update_count
+        _, before = m.dump(sort=False)
+        n_before = int(np.count_nonzero((before & 0xF) == u))
+        m.insert_point_cloud(pts, org, 30.0)
+        _, after = m.dump(sort=False)
+        st = m.last_stats()
+        changed = int(np.count_nonzero((after & 0xF) == u)) - n_before
+        assert st["ray_cells_updated"] == changed - st["cast_rays"]
+
+
+def test_single_pass_and_two_phase_ray_update_agree(gpu, port):
+    """KEEP_NONFINITE maps walk rays in one pass (k_rays); default maps mark
+    and apply. On finite points both give the oracle's map."""
+    scene = synth.LidarScene()
+    a = gpu.ProbabilisticMap(0.1)
+    b = gpu.ProbabilisticMap(0.1, gpu.Config(flags=gpu.FLAG_KEEP_NONFINITE))
+    o = port.pmap(0.1)
+    for k in range(4):
+        pts, org = scene.scan(k, n_points=25000)
+        va = a.insert_point_cloud(pts, org, 30.0)
+        vb = b.insert_point_cloud(pts, org, 30.0)
+        assert va == vb == o.insert(pts, org, 30.0)
+    assert_same_map(a, o)
+    assert_same_map(b, o)

@@ -132,3 +132,49 @@ def test_budget_admission_rejects_and_continues(gpu):
     rq, out = srv.wait_query(t_q, 10)
     assert rq["status"] == 0 and len(out) == 10
     assert srv.stats()["rejected"] == 1
+
+
+def test_insert_waits_for_budget_until_another_map_is_cleared(gpu, port):
+    """An insert that does not fit the HBM budget waits at the head of its
+    map's queue; clearing another client's map (releasing its pools) lets it
+    in, and its result is the same as inserting alone."""
+    scene = synth.LidarScene()
+    pts_a, o_a = scene.scan(0)
+    pts_b, o_b = scene.scan(3)
+    srv = gpu.Server([0.1, 0.1], gpu.ServerConfig(pool_budget_bytes=120 << 20,
+                                                  initial_leaves=4096))
+    try:
+        ra = srv.wait_insert(srv.insert(0, pts_a, o_a, 30.0))
+        assert ra["status"] == 0
+        tb = srv.insert(1, pts_b, o_b, 30.0)
+        with pytest.raises(gpu.BonxaiError) as ei:  # still waiting for budget
+            srv.wait_insert(tb, timeout=0.5)
+        assert ei.value.status == 4
+        assert srv.stats()["deferred"] >= 1
+        srv.wait_insert(srv.clear(0))
+        rb = srv.wait_insert(tb, timeout=60.0)
+        assert rb["status"] == 0 and srv.stats()["rejected"] == 0
+        o = port.pmap(0.1)
+        assert rb["ray_cells"] == o.insert(pts_b, o_b, 30.0)
+        srv.drain()
+        xb, cb = srv.map_dump(1)
+        ox, oc = o.dump()
+        assert np.array_equal(xb, ox) and np.array_equal(cb, oc)
+        xa, _ = srv.map_dump(0)
+        assert len(xa) == 0  # cleared
+    finally:
+        srv.close()
+
+
+def test_insert_that_never_fits_fails_at_its_deadline(gpu):
+    scene = synth.LidarScene()
+    pts, o = scene.scan(0)
+    srv = gpu.Server([0.1], gpu.ServerConfig(pool_budget_bytes=24 << 20, initial_leaves=4096,
+                                             admission_timeout_s=0.3))
+    try:
+        r = srv.wait_insert(srv.insert(0, pts, o, 30.0), timeout=30.0)
+        assert r["status"] == 2  # BXG_ERR_OUT_OF_POOL
+        assert r["latency_ms"] >= 250.0
+        assert srv.stats()["rejected"] == 1
+    finally:
+        srv.close()
