@@ -143,8 +143,8 @@ def peaks():
 
 
 def ncu_traffic():
-    """Per-launch DRAM bytes of the ray kernel from the committed ncu summary."""
-    p = ROOT / "profiles" / "k_rays_lidar_traffic.json"
+    """Per-scan DRAM bytes of the ray phase from the committed ncu summary."""
+    p = ROOT / "profiles" / "ray_phase_lidar_traffic.json"
     if p.exists():
         try:
             return json.loads(p.read_text())
@@ -365,7 +365,7 @@ def run_ours(args):
     achieved = bytes_per_launch / (avg_ray_ms / 1e3) / 1e9
     tr = ncu_traffic()
     roofline = {
-        "kernel": f"k_rays<{32 // max(args.rays_per_warp, 1)},{args.ray_unroll}> (ray phase)",
+        "kernel": "k_mark + k_apply_rays (ray phase: mark the ray cells, apply per leaf)",
         "bound": "hbm", "achieved": achieved,
         "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
         "traffic": tr.get("dram_bytes_per_launch") if tr else None,

@@ -650,12 +650,12 @@ class Batch(_Handle):
     def stats(self) -> dict:
         out = (C.c_double * 8)()
         self._check(self.lib.bxg_batch_stats(self.h, out))
-        ph = (C.c_double * 5)()
+        ph = (C.c_double * 6)()
         self._check(self.lib.bxg_batch_phase_ms(self.h, ph))
         return {"device_ms": out[0], "graph": bool(out[1]), "retried_maps": int(out[2]),
                 "ticks": int(out[3]), "grid": int(out[4]), "launches": int(out[5]),
                 "phase_ms": {"clear": ph[0], "endpoints": ph[1], "winners": ph[2],
-                             "prefix": ph[3], "rays": ph[4]}}
+                             "prefix": ph[3], "rays": ph[4], "rays_mark": ph[5]}}
 
 
 class ServerConfig(C.Structure):

@@ -304,6 +304,7 @@ __global__ void __launch_bounds__(256, U == 2 ? 3 : 4) k_tick(const TickArgs* __
         atomicAdd(A.stats + 4 * s + 2, static_cast<unsigned long long>(visited));
     }
     if (!grid_barrier(A.bar, A.err)) return;
+    stamp(6);
     // 4b: apply, 16 lanes per marked leaf block; each scan's list is taken in
     // a rotated order so that its first entries do not always go to the same
     // groups
@@ -411,7 +412,7 @@ struct bxg_batch_s {
   uint64_t graph_key[7] = {0};
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   float last_ms = 0;
-  double phase_ms[5] = {0, 0, 0, 0, 0};
+  double phase_ms[6] = {0, 0, 0, 0, 0, 0};  // [5]: the mark part of the ray phase
   uint64_t last_retries = 0, ticks = 0, launches = 0;
   std::string err;
   ~bxg_batch_s() {
@@ -736,6 +737,7 @@ int bxg_batch_insert_f32(bxg_batch b, const bxg_pmap* maps, size_t n_scans, cons
   {
     const unsigned long long* ts = reinterpret_cast<const unsigned long long*>(b->h_back + kOffTime);
     for (int k = 0; k < 5; k++) b->phase_ms[k] = double(ts[k + 1] - ts[k]) * 1e-6;
+    b->phase_ms[5] = mark ? double(ts[6] - ts[4]) * 1e-6 : 0.0;
   }
   const unsigned long long* stats =
       reinterpret_cast<const unsigned long long*>(b->h_back + kOffStats);
@@ -778,9 +780,9 @@ int bxg_batch_insert_f32(bxg_batch b, const bxg_pmap* maps, size_t n_scans, cons
   return status;
 }
 
-int bxg_batch_phase_ms(bxg_batch b, double out[5]) {
+int bxg_batch_phase_ms(bxg_batch b, double out[6]) {
   if (!b || !out) return BXG_ERR_INVALID_ARG;
-  for (int k = 0; k < 5; k++) out[k] = b->phase_ms[k];
+  for (int k = 0; k < 6; k++) out[k] = b->phase_ms[k];
   return BXG_OK;
 }
 

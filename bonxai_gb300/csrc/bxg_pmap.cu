@@ -616,9 +616,11 @@ int finish_scan(bxg_pmap_s* pm, int ox, int oy, int oz, bool cast_rays, uint64_t
   int st = BXG_OK;
   for (int attempt = 0; attempt < 12; attempt++) {
     if (attempt) {
-      // retries recount the ray statistics
+      // a retry walks every ray again (recount the visits) but updates only
+      // the cells the failed attempt could not reach: the updated-cell count
+      // adds up over the attempts
       unsigned long long* s = stats_of(m);
-      BXG_CUDA(m, cudaMemsetAsync(s + S_VISITED, 0, 16, m->stream));
+      BXG_CUDA(m, cudaMemsetAsync(s + S_VISITED, 0, 8, m->stream));
     }
     if (attempt) {  // the winners applied the endpoints; complete them after growth
       st = launch_apply(pm);

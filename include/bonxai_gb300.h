@@ -357,8 +357,9 @@ int bxg_batch_insert_f32(bxg_batch b, const bxg_pmap* maps, size_t n_scans, cons
  * launches so far, [6] endpoint phase ms, [7] winner + ray phases ms. */
 int bxg_batch_stats(bxg_batch b, double out[8]);
 /* Last tick's phases in ms (device global timer): [0] clear, [1] endpoints,
- * [2] winners, [3] ray-list prefix, [4] rays. */
-int bxg_batch_phase_ms(bxg_batch b, double out[5]);
+ * [2] winners, [3] ray-list prefix, [4] rays, [5] the marking part of [4]
+ * (two-phase form; 0 otherwise). */
+int bxg_batch_phase_ms(bxg_batch b, double out[6]);
 
 /* ========================================================================
  * Serving: many clients, each with a persistent map on the device, sending

@@ -151,6 +151,7 @@ static int tree(const std::string& out) {
         vsum += leaf_grid.cell(*leaf);
         if (copy && copy->cell(*leaf) != leaf_grid.cell(*leaf)) leaf_copies_match = false;
       }
+      ca.releasePointers();  // one leaf copy at a time: the accessor caps live copies
     }
   }
   long long fsum = 0;
