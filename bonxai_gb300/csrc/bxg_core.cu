@@ -20,7 +20,7 @@ __global__ void k_fill_u32(uint32_t* p, uint32_t v, size_t n) {
 }
 
 // Re-inserts the old root buckets into a larger, empty table.
-__global__ void k_rehash(const uint4* __restrict__ old_b, uint32_t old_cap, DMap M) {
+__global__ void k_rehash(const uint4* __restrict__ old_b, uint32_t old_cap, const __grid_constant__ DMap M) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= old_cap) return;
   const uint4 b = old_b[i];
@@ -49,7 +49,7 @@ __global__ void k_count_on(const unsigned long long* __restrict__ lmask, size_t 
 // word writes the coordinates (and values) of its on cells. mode 0 = every
 // cell; 1 = ProbabilisticMap cells with probability_log > thr; 2 = < thr.
 template <int ESZ>
-__global__ void k_dump(DMap M, uint32_t n_leaves, int32_t* __restrict__ out_xyz,
+__global__ void k_dump(const __grid_constant__ DMap M, uint32_t n_leaves, int32_t* __restrict__ out_xyz,
                        uint8_t* __restrict__ out_val, size_t cap,
                        unsigned long long* __restrict__ counter, int mode, int32_t thr) {
   const size_t t = blockIdx.x * size_t(blockDim.x) + threadIdx.x;

@@ -41,7 +41,7 @@ __global__ void k_pos_to_coord(const uint8_t* __restrict__ pts, size_t stride, u
 // Scratch dedup table: bucket {x, y, z, kept index}; all-ones = empty (a real
 // entry never holds index 0xFFFFFFFF). tab_min (optional) gets the lowest index.
 template <bool KEEP_MAX>
-__global__ void k_dedup_insert(DMap M, const int32_t* __restrict__ xyz, uint32_t n,
+__global__ void k_dedup_insert(const __grid_constant__ DMap M, const int32_t* __restrict__ xyz, uint32_t n,
                                uint4* tab, uint32_t tmask, uint32_t* tab_min) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -79,7 +79,7 @@ __device__ __forceinline__ uint32_t dedup_find(const uint4* tab, uint32_t tmask,
 // Records, for the first item of each cell, whether the cell is on before the
 // batch. It runs before the (retryable) write kernel, so a retry after pool
 // growth cannot change what the first call observed.
-__global__ void k_pre_on(DMap M, const int32_t* __restrict__ xyz, uint32_t n,
+__global__ void k_pre_on(const __grid_constant__ DMap M, const int32_t* __restrict__ xyz, uint32_t n,
                          const uint4* __restrict__ tab, uint32_t tmask,
                          const uint32_t* __restrict__ tab_first, uint8_t* pre) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -109,7 +109,7 @@ __device__ __forceinline__ void copy_val(uint8_t* dst, const uint8_t* src) {
 
 // setValue for the kept (highest-index) item of each cell (bonxai.hpp:449-466).
 template <int ESZ>
-__global__ void k_set_values(DMap M, const int32_t* __restrict__ xyz,
+__global__ void k_set_values(const __grid_constant__ DMap M, const int32_t* __restrict__ xyz,
                              const uint8_t* __restrict__ vals, uint32_t n,
                              const uint4* __restrict__ tab, uint32_t tmask) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -145,7 +145,7 @@ __global__ void k_was_on_first(const int32_t* __restrict__ xyz, uint32_t n,
 // setCellOn for the first item of each cell (bonxai.hpp:537-553): the default
 // is written only if the cell was off.
 template <int ESZ>
-__global__ void k_set_on(DMap M, const int32_t* __restrict__ xyz, uint32_t n,
+__global__ void k_set_on(const __grid_constant__ DMap M, const int32_t* __restrict__ xyz, uint32_t n,
                          const uint8_t* __restrict__ dflt, const uint4* __restrict__ tab,
                          uint32_t tmask) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -164,7 +164,7 @@ __global__ void k_set_on(DMap M, const int32_t* __restrict__ xyz, uint32_t n,
 // setCellOff for the first item of each cell (bonxai.hpp:556-569). The value
 // is zeroed to keep the off-cells-hold-T{} invariant (not observable).
 template <int ESZ>
-__global__ void k_set_off(DMap M, const int32_t* __restrict__ xyz, uint32_t n,
+__global__ void k_set_off(const __grid_constant__ DMap M, const int32_t* __restrict__ xyz, uint32_t n,
                           const uint4* __restrict__ tab, uint32_t tmask, uint8_t* out) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -188,7 +188,7 @@ __global__ void k_set_off(DMap M, const int32_t* __restrict__ xyz, uint32_t n,
 
 // value(coord, create) / ConstAccessor::value / isCellOn (bonxai.hpp:469-534).
 template <int ESZ>
-__global__ void k_get_values(DMap M, const int32_t* __restrict__ xyz, uint32_t n, int create,
+__global__ void k_get_values(const __grid_constant__ DMap M, const int32_t* __restrict__ xyz, uint32_t n, int create,
                              uint8_t* __restrict__ out_vals, uint8_t* __restrict__ found) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -218,7 +218,7 @@ __global__ void k_get_values(DMap M, const int32_t* __restrict__ xyz, uint32_t n
 
 // Write-back of a mutable visitor: only cells that are on take the value.
 template <int ESZ>
-__global__ void k_store_if_on(DMap M, const int32_t* __restrict__ xyz,
+__global__ void k_store_if_on(const __grid_constant__ DMap M, const int32_t* __restrict__ xyz,
                               const uint8_t* __restrict__ vals, uint32_t n) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -233,7 +233,7 @@ __global__ void k_store_if_on(DMap M, const int32_t* __restrict__ xyz,
 
 // releaseUnusedMemory (bonxai.hpp:367-387): leaves whose mask is all off are
 // unlinked from their inner node and pushed on the free stack.
-__global__ void k_release_leaves(DMap M, uint32_t n_leaves) {
+__global__ void k_release_leaves(const __grid_constant__ DMap M, uint32_t n_leaves) {
   const uint32_t lf = blockIdx.x * blockDim.x + threadIdx.x;
   if (lf >= n_leaves) return;
   const int4 key = M.lkey[lf];
@@ -253,7 +253,7 @@ __global__ void k_release_leaves(DMap M, uint32_t n_leaves) {
 // Roots whose inner node has no leaf left are removed. Removal from an
 // open-addressing table would break probe chains, so the surviving buckets
 // are re-inserted into a cleared table (k_rehash) by the host afterwards.
-__global__ void k_drop_empty_roots(DMap M, uint4* out_b, uint32_t cap, uint32_t* kept) {
+__global__ void k_drop_empty_roots(const __grid_constant__ DMap M, uint4* out_b, uint32_t cap, uint32_t* kept) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= cap) return;
   uint4 b = M.buckets[i];
@@ -287,7 +287,7 @@ int check_grid(bxg_grid g) { return g ? BXG_OK : BXG_ERR_INVALID_ARG; }
 // holding (x, y, z) as being created (kPending) by a creator that never
 // publishes, so every access to that leaf waits out its spin limit and sets
 // ERR_WAIT. *held = 1 when the slot was empty and is now held.
-__global__ void k_hold_leaf(DMap M, int x, int y, int z, int* held) {
+__global__ void k_hold_leaf(const __grid_constant__ DMap M, int x, int y, int z, int* held) {
   *held = 0;
   const int32_t rm = root_mask(M);
   const uint32_t in = root_get_or_create(M, x & rm, y & rm, z & rm);
@@ -301,7 +301,7 @@ __global__ void k_hold_leaf(DMap M, int x, int y, int z, int* held) {
 // when the leaf exists, its mask words and all its cell values into out:
 // [int flags][pad][inner mask words][leaf mask words][cells]. flags bit 0: the
 // root exists; bit 1: the leaf exists. Missing parts are written as zeros.
-__global__ void k_read_leaf(DMap M, int x, int y, int z, uint8_t* out) {
+__global__ void k_read_leaf(const __grid_constant__ DMap M, int x, int y, int z, uint8_t* out) {
   __shared__ uint32_t s_in, s_leaf;
   if (threadIdx.x == 0) {
     const int32_t rm = root_mask(M);

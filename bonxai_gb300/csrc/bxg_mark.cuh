@@ -71,19 +71,17 @@ __device__ __forceinline__ void mark_touch(const RayCube& Q, uint32_t b, const D
     set_err(M, ERR_SCRATCH);
 }
 
-// Shared-memory word of cube word w if its leaf is within NB of the origin's
-// leaf (relative leaf coordinates l0x.. of the neighbourhood's corner), else -1.
+// Shared-memory word of the cell (cx, cy, cz) (cube-relative) with bitmap
+// word index wi (0..15 in its leaf) if its leaf is within NB of the origin's
+// leaf (l0x..: the neighbourhood's corner, relative leaf coordinates), else -1.
 template <int NB>
-__device__ __forceinline__ int mark_local(const RayCube& Q, uint32_t w, int l0x, int l0y,
+__device__ __forceinline__ int mark_local(int cx, int cy, int cz, uint32_t wi, int l0x, int l0y,
                                           int l0z) {
   constexpr int NS = 2 * NB + 1;
-  const uint32_t b = w >> 4;
-  const uint32_t SS = Q.S * Q.S;
-  const int bz = int(b / SS), rem = int(b - uint32_t(bz) * SS);
-  const int by = rem / int(Q.S), bx = rem - by * int(Q.S);
-  const unsigned qx = unsigned(bx - l0x), qy = unsigned(by - l0y), qz = unsigned(bz - l0z);
+  const unsigned qx = unsigned((cx >> 3) - l0x), qy = unsigned((cy >> 3) - l0y),
+                 qz = unsigned((cz >> 3) - l0z);
   if (qx < unsigned(NS) && qy < unsigned(NS) && qz < unsigned(NS))
-    return int(((qz * NS + qy) * NS + qx) * 16 + (w & 15));
+    return int(((qz * NS + qy) * NS + qx) * 16 + wi);
   return -1;
 }
 
@@ -107,8 +105,8 @@ __device__ __forceinline__ void mark_rays_block(const DMap& M, const RayCube& Q,
   if (threadIdx.x == 0) *s_next = r0;
   __syncthreads();
   uint32_t last_b = kNone;  // last block this lane ORed into (touch once per run)
-  auto flush = [&](uint32_t w, uint32_t acc) {
-    const int li = mark_local<NB>(Q, w, l0x, l0y, l0z);
+  // w: bitmap word; li: its shared-memory word (-1: global)
+  auto flush = [&](uint32_t w, uint32_t acc, int li) {
     if (li >= 0) {
       atomicOr(sm + li, acc);
       return;
@@ -169,6 +167,7 @@ __device__ __forceinline__ void mark_rays_block(const DMap& M, const RayCube& Q,
       int cx = ox + sx * int(nx) - Q.x0, cy = oy + sy * int(ny) - Q.y0,
           cz = oz + sz * int(nz) - Q.z0;
       uint32_t cur = kNone, acc = 0;
+      int cur_local = -1;
       visited += n;
       for (uint32_t i = 0; i < n; ++i) {
         if (uint32_t(cx) >= side || uint32_t(cy) >= side || uint32_t(cz) >= side) {
@@ -180,9 +179,10 @@ __device__ __forceinline__ void mark_rays_block(const DMap& M, const RayCube& Q,
         const uint32_t li = uint32_t(cx & 7) | (uint32_t(cy & 7) << 3) | (uint32_t(cz & 7) << 6);
         const uint32_t w = b * 16u + (li >> 5);
         if (w != cur) {
-          if (cur != kNone) flush(cur, acc);
+          if (cur != kNone) flush(cur, acc, cur_local);
           cur = w;
           acc = 0;
+          cur_local = mark_local<NB>(cx, cy, cz, li >> 5, l0x, l0y, l0z);
         }
         acc |= 1u << (li & 31);
         rx += 2u * ax;
@@ -201,7 +201,7 @@ __device__ __forceinline__ void mark_rays_block(const DMap& M, const RayCube& Q,
           cz += sz;
         }
       }
-      if (cur != kNone) flush(cur, acc);
+      if (cur != kNone) flush(cur, acc, cur_local);
     }
   }
   // the neighbourhood's words into the bitmap, once per block task
@@ -220,11 +220,25 @@ __device__ __forceinline__ void mark_rays_block(const DMap& M, const RayCube& Q,
 
 // Leaf slot of the leaf whose lowest cell is (lx, ly, lz), created if
 // missing, for a group of kApplyGroup lanes (sl = lane in group, gmask = the
-// group's lanes). The root bucket is probed cooperatively, one bucket per
-// lane; a missing or pending root, a long chain or a missing leaf goes
-// through the bounded-wait creation path on the group's first lane.
+// group's lanes). With a leaf directory D (bxg_scan.cuh), a current word there
+// gives the slot in one load; otherwise the root bucket is probed
+// cooperatively, one bucket per lane, and a missing or pending root, a long
+// chain or a missing leaf goes through the bounded-wait creation path on the
+// group's first lane; the slot found is then written to the directory.
 __device__ __forceinline__ uint32_t apply_leaf_slot(const DMap& M, int lx, int ly, int lz,
-                                                    unsigned sl, unsigned gbase, unsigned gmask) {
+                                                    unsigned sl, unsigned gbase, unsigned gmask,
+                                                    const LeafDir* D) {
+  uint32_t* dw = nullptr;
+  if (D) {
+    const uint32_t qx = static_cast<uint32_t>((lx >> 3) - D->x0),
+                   qy = static_cast<uint32_t>((ly >> 3) - D->y0),
+                   qz = static_cast<uint32_t>((lz >> 3) - D->z0);
+    if (qx < D->side && qy < D->side && qz < D->side) {
+      dw = D->words + (static_cast<size_t>(qx) * D->side + qy) * D->side + qz;
+      const uint32_t w = *dw;
+      if ((w >> 28) == D->epoch) return w & 0x0FFFFFFFu;
+    }
+  }
   const int32_t rm = root_mask(M);
   const int rx = lx & rm, ry = ly & rm, rz = lz & rm;
   const uint32_t h0 = root_hash(M, rx, ry, rz);
@@ -248,6 +262,7 @@ __device__ __forceinline__ uint32_t apply_leaf_slot(const DMap& M, int lx, int l
       leaf = M.ichild[static_cast<size_t>(in) * M.isize + ii];
       if (leaf >= kPending) leaf = leaf_get_or_create(M, in, ii, lx, ly, lz);
     }
+    if (dw && leaf != kNone) *dw = (D->epoch << 28) | leaf;
   }
   return __shfl_sync(gmask, leaf, 0, kApplyGroup);
 }
@@ -259,13 +274,14 @@ __device__ __forceinline__ uint32_t apply_leaf_slot(const DMap& M, int lx, int l
 // pools grew marks its rays again.
 __device__ __forceinline__ void apply_block(const DMap& M, const RayCube& Q, uint32_t b,
                                             int32_t u, int32_t miss, int32_t cmin, unsigned sl,
-                                            unsigned gbase, unsigned gmask, uint32_t& updated) {
+                                            unsigned gbase, unsigned gmask, uint32_t& updated,
+                                            const LeafDir* D = nullptr) {
   const uint32_t SS = Q.S * Q.S;
   const uint32_t bz = b / SS, rem = b - bz * SS, by = rem / Q.S, bx = rem - by * Q.S;
   const int lx = Q.x0 + 8 * int(bx), ly = Q.y0 + 8 * int(by), lz = Q.z0 + 8 * int(bz);
   uint32_t* wp = Q.bits + size_t(b) * 16u + sl;
   const uint32_t w = *wp;
-  const uint32_t leaf = apply_leaf_slot(M, lx, ly, lz, sl, gbase, gmask);
+  const uint32_t leaf = apply_leaf_slot(M, lx, ly, lz, sl, gbase, gmask, D);
   if (sl == 0) atomicAnd(Q.touched + (b >> 5), ~(1u << (b & 31)));
   if (w == 0) return;
   *wp = 0u;

@@ -46,7 +46,7 @@ __device__ __forceinline__ void zero_scan_stats(const DMap& M, int zero) {
 }
 
 template <typename PT>
-__global__ void k_endpoints(DMap M, const uint8_t* __restrict__ pts, size_t stride, uint32_t n,
+__global__ void k_endpoints(const __grid_constant__ DMap M, const uint8_t* __restrict__ pts, size_t stride, uint32_t n,
                             double fx, double fy, double fz, double max_range, double mr2,
                             double inv_res, int keep_nonfinite, int4* __restrict__ ep,
                             uint4* tab, uint32_t tmask, int zero_stats, EpFast F) {
@@ -87,7 +87,7 @@ __device__ __forceinline__ float xf_row(const Xf& t, int r, float x, float y, fl
                    t.m[4 * r + 3]);
 }
 
-__global__ void k_endpoints_sensor(DMap M, const uint8_t* __restrict__ pts, size_t stride,
+__global__ void k_endpoints_sensor(const __grid_constant__ DMap M, const uint8_t* __restrict__ pts, size_t stride,
                                    uint32_t n, Xf xf, double fx, double fy, double fz,
                                    double max_range, double mr2, double inv_res,
                                    int4* __restrict__ ep, uint4* tab, uint32_t tmask,
@@ -109,7 +109,7 @@ __global__ void k_endpoints_sensor(DMap M, const uint8_t* __restrict__ pts, size
 
 // addHitPoint / addMissPoint batches: double points with a given kind, or a
 // per-point kind (0 hit, 1 miss) when kinds != nullptr.
-__global__ void k_endpoints_kind(DMap M, const double* __restrict__ pts, uint32_t n, int kind,
+__global__ void k_endpoints_kind(const __grid_constant__ DMap M, const double* __restrict__ pts, uint32_t n, int kind,
                                  const uint8_t* __restrict__ kinds, double inv_res,
                                  int4* __restrict__ ep, uint4* tab, uint32_t tmask, int zero) {
   zero_scan_stats(M, zero);
@@ -127,7 +127,7 @@ __global__ void k_endpoints_kind(DMap M, const double* __restrict__ pts, uint32_
 // (winner_apply) and, if its ray is cast, joins the ray list.
 // One block-wide atomic each for the ray list, the point count and the ray
 // lengths (a per-warp atomic on three shared counters serialised in L2).
-__global__ void __launch_bounds__(256) k_winners(DMap M, const int4* __restrict__ ep, uint32_t n,
+__global__ void __launch_bounds__(256) k_winners(const __grid_constant__ DMap M, const int4* __restrict__ ep, uint32_t n,
                           const uint4* __restrict__ tab, uint32_t tmask, int ox, int oy, int oz,
                           int32_t u, Opts o, int4* __restrict__ cast, uint32_t cast_cap) {
   __shared__ uint32_t s_cnt[8], s_pts[8], s_base;
@@ -181,7 +181,7 @@ __global__ void __launch_bounds__(256) k_winners(DMap M, const int4* __restrict_
 // Completes listed endpoints after a pool ran out: creates each cell and
 // applies its hit or miss (probabilistic_map.cpp:35-41,49-54). Idempotent --
 // a cell already at u is left alone -- so it may run over the whole list.
-__global__ void k_apply(DMap M, const int4* __restrict__ cast, uint32_t cast_cap, int32_t u,
+__global__ void k_apply(const __grid_constant__ DMap M, const int4* __restrict__ cast, uint32_t cast_cap, int32_t u,
                         Opts o) {
   const uint32_t n = min(ld_volatile(M.ctr + C_CAST), cast_cap);
   for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
@@ -206,7 +206,7 @@ __global__ void k_apply(DMap M, const int4* __restrict__ cast, uint32_t cast_cap
 // Also clears tab[0, tab_n), the endpoint dedup table of the scan, so that
 // the next scan's endpoint phase starts from an empty table without a memset.
 template <int W, int U>
-__global__ void __launch_bounds__(U == 2 ? 256 : 1024, U == 2 ? 3 : 1) k_rays(DMap M, const int4* __restrict__ cast,
+__global__ void __launch_bounds__(U == 2 ? 256 : 1024, U == 2 ? 3 : 1) k_rays(const __grid_constant__ DMap M, const int4* __restrict__ cast,
                                                  uint32_t cast_cap, int ox, int oy, int oz,
                                                  int32_t u, int32_t miss, int32_t cmin,
                                                  uint4* __restrict__ tab, uint32_t tab_n,
@@ -240,7 +240,7 @@ __global__ void __launch_bounds__(U == 2 ? 256 : 1024, U == 2 ? 3 : 1) k_rays(DM
 // Mark phase: block tasks of consecutive rays of the list (taken from the
 // counter *task, zero at launch), marked by mark_rays_block. Also clears
 // tab[0, tab_n), the scan's endpoint dedup table, for the next scan.
-__global__ void __launch_bounds__(1024) k_mark(DMap M, RayCube Q, const int4* __restrict__ cast,
+__global__ void __launch_bounds__(1024) k_mark(const __grid_constant__ DMap M, RayCube Q, const int4* __restrict__ cast,
                                                uint32_t cast_cap, int ox, int oy, int oz,
                                                uint4* __restrict__ tab, uint32_t tab_n,
                                                uint32_t* task) {
@@ -250,8 +250,10 @@ __global__ void __launch_bounds__(1024) k_mark(DMap M, RayCube Q, const int4* __
     tab[t] = make_uint4(kNone, kNone, kNone, kNone);
   for (int t = threadIdx.x; t < kMarkSmemWords; t += blockDim.x) sm[t] = 0u;
   const uint32_t n_cast = min(ld_volatile(M.ctr + C_CAST), cast_cap);
-  // about four tasks per block, at least 64 rays each
-  const uint32_t chunk = max(64u, (n_cast + 4u * gridDim.x - 1) / (4u * gridDim.x));
+  // one task per block (a task ends with a block barrier and the block's
+  // shared-memory flush), at least one four-ray round for every warp
+  const uint32_t min_chunk = (blockDim.x / 32u) * kMarkWarpRays;
+  const uint32_t chunk = max(min_chunk, (n_cast + gridDim.x - 1) / gridDim.x);
   const uint32_t n_tasks = (n_cast + chunk - 1) / chunk;
   uint32_t visited = 0;
   for (;;) {
@@ -270,9 +272,10 @@ __global__ void __launch_bounds__(1024) k_mark(DMap M, RayCube Q, const int4* __
               static_cast<unsigned long long>(visited));
 }
 
-// Apply phase: a group of kApplyGroup lanes per listed leaf block.
-__global__ void __launch_bounds__(256) k_apply_rays(DMap M, RayCube Q, int32_t u, int32_t miss,
-                                                    int32_t cmin) {
+// Apply phase: a group of kApplyGroup lanes per listed leaf block; D: the
+// map's leaf directory (D.words == nullptr: none).
+__global__ void __launch_bounds__(256) k_apply_rays(const __grid_constant__ DMap M, RayCube Q, int32_t u, int32_t miss,
+                                                    int32_t cmin, LeafDir D) {
   const uint32_t n = min(ld_volatile(Q.count), Q.cap);
   const unsigned lane = threadIdx.x & 31;
   const unsigned sl = lane & (kApplyGroup - 1), gbase = lane & ~unsigned(kApplyGroup - 1);
@@ -281,7 +284,8 @@ __global__ void __launch_bounds__(256) k_apply_rays(DMap M, RayCube Q, int32_t u
   const uint32_t ng = (gridDim.x * blockDim.x) / kApplyGroup;
   uint32_t updated = 0;
   for (uint32_t i = gid; i < n; i += ng)
-    apply_block(M, Q, Q.list[i], u, miss, cmin, sl, gbase, gmask, updated);
+    apply_block(M, Q, Q.list[i], u, miss, cmin, sl, gbase, gmask, updated,
+                D.words ? &D : nullptr);
   updated = __reduce_add_sync(0xffffffffu, updated);
   if (lane == 0 && updated)
     atomicAdd(reinterpret_cast<unsigned long long*>(M.ctr + C_STATS) + S_UPDATED,
@@ -289,7 +293,7 @@ __global__ void __launch_bounds__(256) k_apply_rays(DMap M, RayCube Q, int32_t u
 }
 
 // isOccupied / isUnknown / isFree (probabilistic_map.cpp:56-75).
-__global__ void k_query(DMap M, const int32_t* __restrict__ xyz, uint32_t n, int mode,
+__global__ void k_query(const __grid_constant__ DMap M, const int32_t* __restrict__ xyz, uint32_t n, int mode,
                         int32_t thr, uint8_t* __restrict__ out) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -567,7 +571,11 @@ int launch_rays(bxg_pmap_s* pm, int ox, int oy, int oz) {
       const uint64_t groups = std::min<uint64_t>(Q.cap, pm->cast_ub * 64);
       const unsigned ablocks = unsigned(std::min<uint64_t>(uint64_t(m->sm_count) * 8,
                                                            std::max<uint64_t>(1, (groups + 15) / 16)));
-      k_apply_rays<<<ablocks, 256, 0, m->stream>>>(m->dm, Q, pm->update_count, o.miss, o.cmin);
+      LeafDir dir{};
+      st = leaf_dir_for_scan(pm, ox, oy, oz, &dir, size_t(1) << 24, m->stream);
+      if (st) return st;
+      k_apply_rays<<<ablocks, 256, 0, m->stream>>>(m->dm, Q, pm->update_count, o.miss, o.cmin,
+                                                   dir);
       BXG_LAUNCHED(m);
       m->dedup_clean = std::max(m->dedup_clean, tab_n);
       m->dedup_used = 0;
@@ -812,7 +820,7 @@ int add_points(bxg_pmap m_, const double* xyz, size_t n, int kind,
 // xyz (the PCLPoint the node publishes). One thread per leaf mask word; a
 // warp reserves its output range with one atomic. Order is unspecified, as
 // the reference's unordered_map order is.
-__global__ void k_export_occupied(DMap M, uint32_t n_leaves, float* __restrict__ out, size_t cap,
+__global__ void k_export_occupied(const __grid_constant__ DMap M, uint32_t n_leaves, float* __restrict__ out, size_t cap,
                                   unsigned long long* __restrict__ counter, int32_t thr,
                                   double res, double min_z, double max_z) {
   const size_t t = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
