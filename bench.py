@@ -890,9 +890,10 @@ def run_multimap(args):
     log(f"rank {rank}: generated {args.maps} base scans in {time.perf_counter() - t0:.1f} s, "
         f"{sum(len(b[0]) for b in base)} of its points per tick")
     ticks = args.warmup + args.steps
-    big = bx.Config(initial_leaves=1 << 16, initial_inners=1 << 12, hash_buckets=1 << 14)
-    timed_cfg = bx.Config(flags=bx.FLAG_TIMING, initial_leaves=1 << 16, initial_inners=1 << 12,
-                          hash_buckets=1 << 14)
+    big = bx.Config(flags=args.flags, initial_leaves=1 << 16, initial_inners=1 << 12,
+                    hash_buckets=1 << 14)
+    timed_cfg = bx.Config(flags=bx.FLAG_TIMING | args.flags, initial_leaves=1 << 16,
+                          initial_inners=1 << 12, hash_buckets=1 << 14)
     bmaps = [bx.ProbabilisticMap(sp.resolution, big) for sp in specs]
     pmaps = [bx.ProbabilisticMap(sp.resolution, timed_cfg) for sp in specs]
     batch = bx.Batch(bx.Config(rays_per_warp=args.rays_per_warp, ray_unroll=args.ray_unroll))

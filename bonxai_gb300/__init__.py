@@ -32,6 +32,7 @@ SET_ALL_CELLS_OFF = 1
 FLAG_KEEP_NONFINITE = 1
 FLAG_TIMING = 2
 FLAG_NO_GRAPH = 4
+FLAG_RAYS_SINGLE_PASS = 8
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "node pool exhausted", 3: "root hash full",
           4: "device wait timed out", 5: "CUDA error", 6: "no CUDA device",

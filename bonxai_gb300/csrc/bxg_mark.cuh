@@ -57,6 +57,27 @@ struct RayCube {
   uint32_t cap;       // list capacity
 };
 
+// Fire-and-forget ORs and AND into global memory. The pointers may reach the
+// code as generic addresses (the batched tick keeps its scan table, with the
+// bitmap and pool pointers, in shared memory), and an atomicOr on a generic
+// address compiles to an atomic that returns its old value, which the warp
+// then waits for; these always issue the reduction form.
+__device__ __forceinline__ void red_or(uint32_t* p, uint32_t v) {
+  asm volatile("red.relaxed.gpu.global.or.b32 [%0], %1;" ::"l"(__cvta_generic_to_global(p)),
+               "r"(v)
+               : "memory");
+}
+__device__ __forceinline__ void red_or64(unsigned long long* p, unsigned long long v) {
+  asm volatile("red.relaxed.gpu.global.or.b64 [%0], %1;" ::"l"(__cvta_generic_to_global(p)),
+               "l"(v)
+               : "memory");
+}
+__device__ __forceinline__ void red_and(uint32_t* p, uint32_t v) {
+  asm volatile("red.relaxed.gpu.global.and.b32 [%0], %1;" ::"l"(__cvta_generic_to_global(p)),
+               "r"(v)
+               : "memory");
+}
+
 // Puts block b on the list the first time any bit of it is set.
 __device__ __forceinline__ void mark_touch(const RayCube& Q, uint32_t b, const DMap& M) {
   uint32_t* tw = Q.touched + (b >> 5);
@@ -111,7 +132,7 @@ __device__ __forceinline__ void mark_rays_block(const DMap& M, const RayCube& Q,
       atomicOr(sm + li, acc);
       return;
     }
-    atomicOr(Q.bits + w, acc);
+    red_or(Q.bits + w, acc);
     const uint32_t b = w >> 4;
     if (b != last_b) {
       last_b = b;
@@ -212,7 +233,7 @@ __device__ __forceinline__ void mark_rays_block(const DMap& M, const RayCube& Q,
     sm[t] = 0;
     const int q = t >> 4, qx = q % NS, qy = (q / NS) % NS, qz = q / (NS * NS);
     const uint32_t b = uint32_t(l0x + qx) + Q.S * (uint32_t(l0y + qy) + Q.S * uint32_t(l0z + qz));
-    atomicOr(Q.bits + b * 16u + (t & 15), v);
+    red_or(Q.bits + b * 16u + (t & 15), v);
     mark_touch(Q, b, M);
   }
   __syncthreads();
@@ -282,7 +303,7 @@ __device__ __forceinline__ void apply_block(const DMap& M, const RayCube& Q, uin
   uint32_t* wp = Q.bits + size_t(b) * 16u + sl;
   const uint32_t w = *wp;
   const uint32_t leaf = apply_leaf_slot(M, lx, ly, lz, sl, gbase, gmask, D);
-  if (sl == 0) atomicAnd(Q.touched + (b >> 5), ~(1u << (b & 31)));
+  if (sl == 0) red_and(Q.touched + (b >> 5), ~(1u << (b & 31)));
   if (w == 0) return;
   *wp = 0u;
   if (leaf == kNone) return;
@@ -310,7 +331,7 @@ __device__ __forceinline__ void apply_block(const DMap& M, const RayCube& Q, uin
     if (changed) cells[j] = v;
   }
   if (fresh)
-    atomicOr(M.lmask + static_cast<size_t>(leaf) * M.lwords + (sl >> 1),
+    red_or64(M.lmask + static_cast<size_t>(leaf) * M.lwords + (sl >> 1),
              static_cast<unsigned long long>(fresh) << (32u * (sl & 1u)));
 }
 

@@ -492,7 +492,9 @@ constexpr uint32_t kMaxCubeSide = 200;
 int cube_for_scan(bxg_pmap_s* pm, int ox, int oy, int oz, double reach, RayCube* Q, bool* ok) {
   MapCore* m = &pm->core;
   *ok = false;
-  if (m->dm.lb != 3 || m->dm.esz != 4 || (m->flags & BXG_FLAG_KEEP_NONFINITE)) return BXG_OK;
+  if (m->dm.lb != 3 || m->dm.esz != 4 ||
+      (m->flags & (BXG_FLAG_KEEP_NONFINITE | BXG_FLAG_RAYS_SINGLE_PASS)))
+    return BXG_OK;
   if (!(reach > 0) || !std::isfinite(reach)) return BXG_OK;
   // Ray ends lie within ceil(reach / res) + 2 cells of the origin cell (the
   // floor of the origin and of the end each move a cell by less than one), so

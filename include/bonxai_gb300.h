@@ -76,6 +76,12 @@ typedef struct {
 #define BXG_FLAG_TIMING 2u
 /* Batched ticks: launch directly instead of replaying a captured CUDA graph. */
 #define BXG_FLAG_NO_GRAPH 4u
+/* The ray phase of a scan walks each ray once and updates its cells on the
+ * way (one pass), instead of marking the scan's ray cells in a bitmap and
+ * then updating each marked leaf once (two phases, the default). Same
+ * results; which is faster depends on the scan (the autotuner times both). A
+ * batched tick uses one pass when any of its maps has this flag. */
+#define BXG_FLAG_RAYS_SINGLE_PASS 8u
 
 void bxg_config_default(bxg_config* cfg);
 const char* bxg_status_string(int status);

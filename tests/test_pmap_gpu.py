@@ -442,16 +442,19 @@ def test_ray_phase_counts_each_updated_cell_once(gpu):
 
 
 def test_single_pass_and_two_phase_ray_update_agree(gpu, port):
-    """KEEP_NONFINITE maps walk rays in one pass (k_rays); default maps mark
-    and apply. On finite points both give the oracle's map."""
+    """Maps with FLAG_RAYS_SINGLE_PASS (or KEEP_NONFINITE) walk rays in one pass
+    (k_rays); default maps mark and apply. On finite points all give the
+    oracle's map."""
     scene = synth.LidarScene()
     a = gpu.ProbabilisticMap(0.1)
     b = gpu.ProbabilisticMap(0.1, gpu.Config(flags=gpu.FLAG_KEEP_NONFINITE))
+    c = gpu.ProbabilisticMap(0.1, gpu.Config(flags=gpu.FLAG_RAYS_SINGLE_PASS))
     o = port.pmap(0.1)
     for k in range(4):
         pts, org = scene.scan(k, n_points=25000)
         va = a.insert_point_cloud(pts, org, 30.0)
         vb = b.insert_point_cloud(pts, org, 30.0)
-        assert va == vb == o.insert(pts, org, 30.0)
-    assert_same_map(a, o)
-    assert_same_map(b, o)
+        vc = c.insert_point_cloud(pts, org, 30.0)
+        assert va == vb == vc == o.insert(pts, org, 30.0)
+    for m in (a, b, c):
+        assert_same_map(m, o)
