@@ -1,6 +1,9 @@
 """Autotuner for the ray-phase launch shape and the root-hash load factor.
 
 Tunable knobs (none changes a result, only speed):
+  ray phase       two phases (mark the ray cells, then apply per leaf) or one
+                  pass (BXG_FLAG_RAYS_SINGLE_PASS); the knobs below shape the
+                  one-pass walk
   rays_per_warp   1, 2, 4   lanes per ray = 32 / rays_per_warp
   ray_unroll      1, 2      cells per lane per step
   block_size      0, 256, 1024  threads per block of the per-map ray kernel
@@ -35,17 +38,21 @@ def _lidar_sample(n_scans=6, n_points=131072):
 
 
 def tune_per_map(scans, resolution, max_range, repeats=2):
-    """Best (rays_per_warp, ray_unroll, block_size, hash_load_factor) for the
-    per-map scan, by the summed ray-kernel time over the sample."""
+    """Best (ray-phase form, rays_per_warp, ray_unroll, block_size,
+    hash_load_factor) for the per-map scan, by the summed scan time over the
+    sample."""
     import torch
     import bonxai_gb300 as bx
     dev = [(torch.from_numpy(p).cuda(), o) for p, o in scans]
     results = []
-    for rpw, unroll, bs, lf in itertools.product((1, 2, 4), (1, 2), (0, 256, 1024), (0.25, 0.5, 0.75)):
+    cands = [(0, 1, 1, 0, lf) for lf in (0.25, 0.5, 0.75)]  # two phases
+    cands += [(bx.FLAG_RAYS_SINGLE_PASS,) + c for c in
+              itertools.product((1, 2, 4), (1, 2), (0, 256, 1024), (0.25, 0.5, 0.75))]
+    for form, rpw, unroll, bs, lf in cands:
         best = None
         for _ in range(repeats):
             cfg = bx.Config(rays_per_warp=rpw, ray_unroll=unroll, block_size=bs,
-                            hash_load_factor=lf, flags=bx.FLAG_TIMING,
+                            hash_load_factor=lf, flags=bx.FLAG_TIMING | form,
                             initial_leaves=1 << 18, hash_buckets=1 << 12)
             m = bx.ProbabilisticMap(resolution, cfg)
             t_ray = t_all = 0.0
@@ -56,15 +63,15 @@ def tune_per_map(scans, resolution, max_range, repeats=2):
                 t_all += sum(kt)
             m.close()
             best = t_all if best is None else min(best, t_all)
-        results.append({"rays_per_warp": rpw, "ray_unroll": unroll, "block_size": bs,
-                        "hash_load_factor": lf, "scan_ms": best / len(dev)})
+        results.append({"flags": form, "rays_per_warp": rpw, "ray_unroll": unroll,
+                        "block_size": bs, "hash_load_factor": lf, "scan_ms": best / len(dev)})
     results.sort(key=lambda r: r["scan_ms"])
     return results
 
 
 def tune_batched(n_maps=16, ticks=3):
-    """Best (rays_per_warp, ray_unroll) for the batched tick on a multi-map
-    sample, by device time per tick."""
+    """Best (ray-phase form, rays_per_warp, ray_unroll) for the batched tick on a
+    multi-map sample, by device time per tick."""
     import torch
     import bonxai_gb300 as bx
     from bonxai_gb300 import synth
@@ -82,14 +89,16 @@ def tune_batched(n_maps=16, ticks=3):
     off = np.concatenate([[0], np.cumsum([len(s[0]) for s in scans])]).astype(np.uint64)
     org = np.stack([s[1] for s in scans])
     results = []
-    for rpw, unroll in itertools.product((1, 2, 4), (1, 2)):
+    cands = [(0, 1, 1)] + [(bx.FLAG_RAYS_SINGLE_PASS, rpw, unroll)
+                           for rpw, unroll in itertools.product((1, 2, 4), (1, 2))]
+    for form, rpw, unroll in cands:
         b = bx.Batch(bx.Config(rays_per_warp=rpw, ray_unroll=unroll))
-        maps = [bx.ProbabilisticMap(sp.resolution) for sp in specs]
+        maps = [bx.ProbabilisticMap(sp.resolution, bx.Config(flags=form)) for sp in specs]
         times = []
         for _ in range(ticks):
             b.insert(maps, pts, off, org, 10.0)
             times.append(b.stats()["device_ms"])
-        results.append({"rays_per_warp": rpw, "ray_unroll": unroll,
+        results.append({"flags": form, "rays_per_warp": rpw, "ray_unroll": unroll,
                         "tick_ms": float(np.median(times[1:] if len(times) > 1 else times))})
         for m in maps:
             m.close()

@@ -64,6 +64,7 @@ struct TickScan {
   int32_t keep_nonfinite;
   int32_t pad;
   RayCube Q;  // the map's cube bitmap (two-phase ray update)
+  LeafDir D;  // the map's kept leaf directory (D.words == nullptr: none)
 };
 
 static_assert(sizeof(TickScan) % 8 == 0, "TickScan is copied to shared memory in 8-byte words");
@@ -320,7 +321,8 @@ __global__ void __launch_bounds__(256, U == 2 ? 3 : 4) k_tick(const TickArgs* __
         const uint32_t n = min(ld_volatile(S.Q.count), S.Q.cap);
         uint32_t upd = 0;
         for (uint32_t i = (gid + s * 977u) % ng; i < n; i += ng)
-          apply_block(S.M, S.Q, S.Q.list[i], S.u, S.o.miss, S.o.cmin, sl, gbase, gmask, upd);
+          apply_block(S.M, S.Q, S.Q.list[i], S.u, S.o.miss, S.o.cmin, sl, gbase, gmask, upd,
+                      S.D.words ? &S.D : nullptr);
         if (upd) atomicAdd(s_upd + s, upd);
       }
     }
@@ -678,6 +680,15 @@ int bxg_batch_insert_f32(bxg_batch b, const bxg_pmap* maps, size_t n_scans, cons
     const int st = cube_for_scan(maps[s], S.ox, S.oy, S.oz, S.max_range, &S.Q, &ok);
     if (st) return bfail(b, st, maps[s]->core.err);
     mark = ok;
+  }
+  // each map's kept leaf directory for the apply phase (its memsets go on the
+  // batch's stream, ahead of the tick)
+  for (size_t s = 0; s < n_scans && mark; s++) {
+    TickScan& S = b->h_scans[s];
+    maps[s]->dir_reach = S.max_range;
+    const int st = leaf_dir_for_scan(maps[s], S.ox, S.oy, S.oz, &S.D, size_t(1) << 23, b->stream);
+    maps[s]->dir_reach = 0.0;
+    if (st) return bfail(b, st, maps[s]->core.err);
   }
   b->back_bytes = kBackBytes;
   const size_t param_bytes = 256 + n_scans * sizeof(TickScan);

@@ -16,8 +16,8 @@
 //          memory first and ORed into the bitmap once per block task. The
 //          first OR into a block puts the block on the scan's list
 //          (test-and-set on a per-block bit).
-//   apply  One group of 16 lanes per listed block: a cooperative probe of the
-//          root hash (16 buckets per step), the leaf get-or-create (topology:
+//   apply  One group of 8 lanes per listed block: a cooperative probe of the
+//          root hash (8 buckets per step), the leaf get-or-create (topology:
 //          once per leaf, not once per ray crossing), then the miss update of
 //          the marked cells with vector loads and stores, the mask bits of
 //          cells turned on, and the block cleared for the next scan.
@@ -43,7 +43,7 @@ __host__ __device__ constexpr int mark_smem_words(int nb) {
 }
 constexpr int kMarkSmemWords = mark_smem_words(kMarkNB);
 constexpr uint32_t kMarkWarpRays = 4;  // rays a warp takes at a time
-constexpr int kApplyGroup = 16;        // lanes per listed block in apply
+constexpr int kApplyGroup = 8;         // lanes per listed block in apply (4 blocks per warp)
 
 // The bitmap of one scan. Block b = bx + S*(by + S*bz) covers the cells
 // x0 + 8*bx .. x0 + 8*bx + 7 (likewise y, z).
@@ -288,11 +288,12 @@ __device__ __forceinline__ uint32_t apply_leaf_slot(const DMap& M, int lx, int l
   return __shfl_sync(gmask, leaf, 0, kApplyGroup);
 }
 
-// Applies the ray update to listed block b and clears it (16 lanes, lane sl
-// owns word sl: cells 32*sl .. 32*sl+31 of the 8^3 leaf). The block's bits and
-// list bit are cleared even when the leaf cannot be had (pool full, error set):
-// the bitmap is clean after every apply, and a scan that is re-run after the
-// pools grew marks its rays again.
+// Applies the ray update to listed block b and clears it (8 lanes; lane sl
+// owns bitmap words 2 sl and 2 sl + 1, i.e. the 64 cells 64 sl .. 64 sl + 63
+// of the 8^3 leaf, which are mask word sl). The block's bits and list bit are
+// cleared even when the leaf cannot be had (pool full, error set): the bitmap
+// is clean after every apply, and a scan that is re-run after the pools grew
+// marks its rays again.
 __device__ __forceinline__ void apply_block(const DMap& M, const RayCube& Q, uint32_t b,
                                             int32_t u, int32_t miss, int32_t cmin, unsigned sl,
                                             unsigned gbase, unsigned gmask, uint32_t& updated,
@@ -300,39 +301,41 @@ __device__ __forceinline__ void apply_block(const DMap& M, const RayCube& Q, uin
   const uint32_t SS = Q.S * Q.S;
   const uint32_t bz = b / SS, rem = b - bz * SS, by = rem / Q.S, bx = rem - by * Q.S;
   const int lx = Q.x0 + 8 * int(bx), ly = Q.y0 + 8 * int(by), lz = Q.z0 + 8 * int(bz);
-  uint32_t* wp = Q.bits + size_t(b) * 16u + sl;
-  const uint32_t w = *wp;
+  uint2* wp = reinterpret_cast<uint2*>(Q.bits + size_t(b) * 16u) + sl;
+  const uint2 wv = *wp;
   const uint32_t leaf = apply_leaf_slot(M, lx, ly, lz, sl, gbase, gmask, D);
   if (sl == 0) red_and(Q.touched + (b >> 5), ~(1u << (b & 31)));
-  if (w == 0) return;
-  *wp = 0u;
+  if ((wv.x | wv.y) == 0u) return;
+  *wp = make_uint2(0u, 0u);
   if (leaf == kNone) return;
   int4* cells = reinterpret_cast<int4*>(reinterpret_cast<int32_t*>(M.ldata) +
-                                        static_cast<size_t>(leaf) * 512u + 32u * sl);
-  uint32_t fresh = 0;  // cells whose word was zero: turn their mask bits on
+                                        static_cast<size_t>(leaf) * 512u + 64u * sl);
+  unsigned long long fresh = 0;  // cells whose word was zero: turn their mask bits on
 #pragma unroll
-  for (int j = 0; j < 8; ++j) {
-    const uint32_t nib = (w >> (4 * j)) & 0xFu;
-    if (!nib) continue;
-    int4 v = cells[j];
-    int32_t* c = reinterpret_cast<int32_t*>(&v);
-    bool changed = false;
+  for (int h = 0; h < 2; ++h) {
+    const uint32_t w = h ? wv.y : wv.x;
 #pragma unroll
-    for (int t = 0; t < 4; ++t) {
-      if (!((nib >> t) & 1u)) continue;
-      const int32_t old = c[t];
-      if (cell_id(old) != u) {
-        c[t] = cell_pack(max(wrap_add(cell_prob(old), miss), cmin), u);
-        changed = true;
-        ++updated;
+    for (int j = 0; j < 8; ++j) {
+      const uint32_t nib = (w >> (4 * j)) & 0xFu;
+      if (!nib) continue;
+      int4 v = cells[8 * h + j];
+      int32_t* c = reinterpret_cast<int32_t*>(&v);
+      bool changed = false;
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        if (!((nib >> t) & 1u)) continue;
+        const int32_t old = c[t];
+        if (cell_id(old) != u) {
+          c[t] = cell_pack(max(wrap_add(cell_prob(old), miss), cmin), u);
+          changed = true;
+          ++updated;
+        }
+        if (old == 0) fresh |= 1ull << (32 * h + 4 * j + t);
       }
-      if (old == 0) fresh |= 1u << (4 * j + t);
+      if (changed) cells[8 * h + j] = v;
     }
-    if (changed) cells[j] = v;
   }
-  if (fresh)
-    red_or64(M.lmask + static_cast<size_t>(leaf) * M.lwords + (sl >> 1),
-             static_cast<unsigned long long>(fresh) << (32u * (sl & 1u)));
+  if (fresh) red_or64(M.lmask + static_cast<size_t>(leaf) * M.lwords + sl, fresh);
 }
 
 }  // namespace bxg

@@ -569,10 +569,12 @@ int launch_rays(bxg_pmap_s* pm, int ox, int oy, int oz) {
                                              m->s_dedup.as<uint4>(), tab_n,
                                              m->ctr.as<uint32_t>() + C_TASK);
       BXG_LAUNCHED(m);
-      // 16 groups per 256-thread block; the list holds at most min(cube, 64 x rays) blocks
+      // 256 / kApplyGroup groups per block; the list holds at most
+      // min(cube, 64 x rays) blocks
       const uint64_t groups = std::min<uint64_t>(Q.cap, pm->cast_ub * 64);
-      const unsigned ablocks = unsigned(std::min<uint64_t>(uint64_t(m->sm_count) * 8,
-                                                           std::max<uint64_t>(1, (groups + 15) / 16)));
+      const uint64_t per_block = 256 / kApplyGroup;
+      const unsigned ablocks = unsigned(std::min<uint64_t>(
+          uint64_t(m->sm_count) * 8, std::max<uint64_t>(1, (groups + per_block - 1) / per_block)));
       LeafDir dir{};
       st = leaf_dir_for_scan(pm, ox, oy, oz, &dir, size_t(1) << 24, m->stream);
       if (st) return st;
