@@ -13,7 +13,8 @@
 //   phase 4  the ray phase of all scans. Two-phase form (every map has a
 //            cube bitmap, bxg_mark.cuh): 4a blocks take tasks of consecutive
 //            rays of one scan and mark their cells in that map's bitmap; 4b
-//            groups of 16 lanes apply each map's marked leaves. Single-pass
+//            warps list the marked leaf blocks of every map; 4c groups of 8
+//            lanes apply each map's listed blocks. Single-pass
 //            form otherwise: groups of W lanes walk rays of all scans
 //            (walk_ray), each on its own map's pools. Statistics per scan.
 //   phase 5  each map's counters are copied to one read-back block
@@ -62,7 +63,7 @@ struct TickScan {
   uint32_t n;                    // points
   uint32_t tmask;                // dedup table size - 1
   int32_t keep_nonfinite;
-  int32_t pad;
+  uint32_t chunk0;  // first chunk (32 touched words) of this scan's cube in the tick's list phase
   RayCube Q;  // the map's cube bitmap (two-phase ray update)
   LeafDir D;  // the map's kept leaf directory (D.words == nullptr: none)
 };
@@ -85,7 +86,7 @@ struct TickArgs {
   uint32_t* ctr_out;          // [n_scans][C_WORDS]
   unsigned long long* times;  // [8] global-timer stamps at each phase boundary
   uint32_t n_scans;
-  uint32_t pad;
+  uint32_t n_chunks;  // chunks of 32 touched words over all scans' cubes
   unsigned long long total_points;
   unsigned long long total_tab;
 };
@@ -159,19 +160,28 @@ __device__ __forceinline__ uint32_t scan_of_task(const uint32_t* prefix, uint32_
   return lo;
 }
 
+__device__ __forceinline__ uint32_t scan_of_chunk(const TickScan* sc, uint32_t n, uint32_t c) {
+  uint32_t lo = 0, hi = n;  // last scan with chunk0 <= c
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (sc[mid].chunk0 <= c) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
 // MARK: phase 4 in the two-phase form (every scan has a cube). Dynamic shared
-// memory: the scan table (kMaxTickScans entries), then, with MARK, the mark
+// memory: the scan table (n_scans entries), then, with MARK, the mark
 // neighbourhood (mark_smem_words(kTickMarkNB) words).
 template <int W, int U, bool MARK>
 __global__ void __launch_bounds__(256, U == 2 ? 3 : 4) k_tick(const TickArgs* __restrict__ argp,
                                                  const TickScan* __restrict__ scans_g) {
   extern __shared__ unsigned long long smem_raw[];
   TickScan* sc = reinterpret_cast<TickScan*>(smem_raw);
-  uint32_t* smk = reinterpret_cast<uint32_t*>(smem_raw + kMaxTickScans * (sizeof(TickScan) / 8));
-  __shared__ uint32_t s_next, s_task;
+  __shared__ uint32_t s_task;
   __shared__ uint32_t s_upd[kMaxTickScans];
   const TickArgs A = *argp;
   const uint32_t ns = A.n_scans;
+  uint32_t* smk = reinterpret_cast<uint32_t*>(smem_raw + ns * (sizeof(TickScan) / 8));
   {
     const uint32_t words = ns * (sizeof(TickScan) / 8);
     const unsigned long long* src = reinterpret_cast<const unsigned long long*>(scans_g);
@@ -192,7 +202,7 @@ __global__ void __launch_bounds__(256, U == 2 ? 3 : 4) k_tick(const TickArgs* __
   for (unsigned long long k = gtid; k < ns; k += gsize) {
     A.cast_cnt[k] = 0;
     for (int j = 0; j < 4; j++) A.stats[4 * k + j] = 0;
-    if (MARK) *sc[k].Q.count = 0u;
+    if (MARK) *sc[k].Q.count = 0u;  // the list phase appends from zero
   }
   if (!grid_barrier(A.bar, A.err)) return;
   stamp(1);
@@ -284,6 +294,7 @@ __global__ void __launch_bounds__(256, U == 2 ? 3 : 4) k_tick(const TickArgs* __
   // phase 4: rays of all scans
   if (MARK) {
     // 4a: mark
+    __shared__ MarkRays<256> s_rays;
     for (int t = threadIdx.x; t < mark_smem_words(kTickMarkNB); t += blockDim.x) smk[t] = 0u;
     const uint32_t n_tasks = ld_volatile(A.task_prefix + ns);
     const uint32_t chunk = ld_volatile(A.chunk);
@@ -298,15 +309,24 @@ __global__ void __launch_bounds__(256, U == 2 ? 3 : 4) k_tick(const TickArgs* __
       const uint32_t rays = ld_volatile(A.ray_prefix + s + 1) - ld_volatile(A.ray_prefix + s);
       const uint32_t r0 = (t - ld_volatile(A.task_prefix + s)) * chunk;
       uint32_t visited = 0;
-      mark_rays_block<kTickMarkNB>(S.M, S.Q, A.cast + S.pt_begin, r0, min(rays, r0 + chunk),
-                                   S.ox, S.oy, S.oz, smk, &s_next, visited);
+      mark_rays_block<kTickMarkNB, 256>(S.M, S.Q, A.cast + S.pt_begin, r0, min(rays, r0 + chunk),
+                                        S.ox, S.oy, S.oz, smk, s_rays, visited);
       visited = __reduce_add_sync(0xffffffffu, visited);
       if (lane == 0 && visited)
         atomicAdd(A.stats + 4 * s + 2, static_cast<unsigned long long>(visited));
     }
     if (!grid_barrier(A.bar, A.err)) return;
     stamp(6);
-    // 4b: apply, 16 lanes per marked leaf block; each scan's list is taken in
+    // 4b: the marked blocks of every cube onto its list (a warp per 32
+    // touched words, all scans in one index space)
+    for (uint32_t c = static_cast<uint32_t>(gtid >> 5); c < A.n_chunks;
+         c += static_cast<uint32_t>(gsize >> 5)) {
+      const uint32_t s = scan_of_chunk(sc, ns, c);
+      list_touched(sc[s].M, sc[s].Q, c - sc[s].chunk0);
+    }
+    if (!grid_barrier(A.bar, A.err)) return;
+    stamp(7);
+    // 4c: apply, 8 lanes per listed leaf block; each scan's list is taken in
     // a rotated order so that its first entries do not always go to the same
     // groups
     for (uint32_t k = threadIdx.x; k < ns; k += blockDim.x) s_upd[k] = 0u;
@@ -399,6 +419,7 @@ struct bxg_batch_s {
   int sm_count = 0;
   int grid = 0;       // resident blocks of the single-pass tick
   int grid_mark = 0;  // resident blocks of the two-phase tick
+  size_t grid_smem[2] = {0, 0};  // dynamic shared memory the two were sized for
   bool use_graph = true;
   // device buffers
   DevBuf pts, ep, tab, cast, meta, params;
@@ -462,11 +483,10 @@ int occupancy_grid(bxg_batch b, size_t smem) {
   return per_sm * b->sm_count;
 }
 
-// Dynamic shared memory of a tick: the scan table, plus the mark
+// Dynamic shared memory of a tick of ns scans: the scan table, plus the mark
 // neighbourhood in the two-phase form.
-size_t tick_smem(bool mark) {
-  return kMaxTickScans * sizeof(TickScan) +
-         (mark ? size_t(mark_smem_words(kTickMarkNB)) * 4 : 0);
+size_t tick_smem(bool mark, size_t ns) {
+  return ns * sizeof(TickScan) + (mark ? size_t(mark_smem_words(kTickMarkNB)) * 4 : 0);
 }
 
 template <int W, int U, bool MARK>
@@ -536,7 +556,7 @@ int bxg_batch_create(bxg_batch* out, const bxg_config* cfg_in) {
     delete b;
     return BXG_ERR_CUDA;
   }
-  const int smem = int(tick_smem(false));
+  const int smem = int(tick_smem(false, kMaxTickScans));
   cudaFuncSetAttribute(k_tick<32, 1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   cudaFuncSetAttribute(k_tick<16, 1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   cudaFuncSetAttribute(k_tick<8, 1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
@@ -544,7 +564,7 @@ int bxg_batch_create(bxg_batch* out, const bxg_config* cfg_in) {
   cudaFuncSetAttribute(k_tick<16, 2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   cudaFuncSetAttribute(k_tick<8, 2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   cudaFuncSetAttribute(k_tick<32, 1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       int(tick_smem(true)));
+                       int(tick_smem(true, kMaxTickScans)));
   cudaGetLastError();
   const size_t pbytes = 256 + kMaxTickScans * sizeof(TickScan);
   if (cudaMallocHost(reinterpret_cast<void**>(&b->h_args), pbytes) != cudaSuccess ||
@@ -681,6 +701,13 @@ int bxg_batch_insert_f32(bxg_batch b, const bxg_pmap* maps, size_t n_scans, cons
     if (st) return bfail(b, st, maps[s]->core.err);
     mark = ok;
   }
+  // the list phase's index space: 32 touched words per chunk, scan after scan
+  A.n_chunks = 0;
+  for (size_t s = 0; s < n_scans && mark; s++) {
+    TickScan& S = b->h_scans[s];
+    S.chunk0 = A.n_chunks;
+    A.n_chunks += (cube_touched_words(S.Q) + 31u) / 32u;
+  }
   // each map's kept leaf directory for the apply phase (its memsets go on the
   // batch's stream, ahead of the tick)
   for (size_t s = 0; s < n_scans && mark; s++) {
@@ -692,18 +719,21 @@ int bxg_batch_insert_f32(bxg_batch b, const bxg_pmap* maps, size_t n_scans, cons
   }
   b->back_bytes = kBackBytes;
   const size_t param_bytes = 256 + n_scans * sizeof(TickScan);
-  const size_t smem = tick_smem(mark);
-  if (!b->grid) {
+  const size_t smem = tick_smem(mark, n_scans);
+  // resident blocks for this shared-memory size (the launch is cooperative)
+  if (mark && (!b->grid_mark || b->grid_smem[1] != smem)) {
+    b->grid_mark = occupancy_grid<32, 1, true>(b, smem);
+    b->grid_smem[1] = smem;
+    if (b->grid_mark <= 0) return bfail(b, BXG_ERR_CUDA, "k_tick cannot be resident");
+  } else if (!mark && (!b->grid || b->grid_smem[0] != smem)) {
     const bool u2 = b->ray_unroll == 2;
-    const size_t sm0 = tick_smem(false);
     switch (b->rays_per_warp) {
-      case 4: b->grid = u2 ? occupancy_grid<8, 2, false>(b, sm0) : occupancy_grid<8, 1, false>(b, sm0); break;
-      case 2: b->grid = u2 ? occupancy_grid<16, 2, false>(b, sm0) : occupancy_grid<16, 1, false>(b, sm0); break;
-      default: b->grid = u2 ? occupancy_grid<32, 2, false>(b, sm0) : occupancy_grid<32, 1, false>(b, sm0); break;
+      case 4: b->grid = u2 ? occupancy_grid<8, 2, false>(b, smem) : occupancy_grid<8, 1, false>(b, smem); break;
+      case 2: b->grid = u2 ? occupancy_grid<16, 2, false>(b, smem) : occupancy_grid<16, 1, false>(b, smem); break;
+      default: b->grid = u2 ? occupancy_grid<32, 2, false>(b, smem) : occupancy_grid<32, 1, false>(b, smem); break;
     }
-    b->grid_mark = occupancy_grid<32, 1, true>(b, tick_smem(true));
-    if (b->grid <= 0 || b->grid_mark <= 0)
-      return bfail(b, BXG_ERR_CUDA, "k_tick cannot be resident");
+    b->grid_smem[0] = smem;
+    if (b->grid <= 0) return bfail(b, BXG_ERR_CUDA, "k_tick cannot be resident");
   }
 
   // Run: the captured graph when its shape matches, else capture it again.

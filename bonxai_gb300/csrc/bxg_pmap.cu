@@ -13,10 +13,11 @@
 //                 {cell, hit/miss} to the ray list (and counts the ray length
 //                 for the ray-cell total).
 //   k_apply       only after a pool ran out: completes the listed endpoints.
-//   k_mark        the ray phase's first half: every listed ray's cells set
+//   k_mark        the ray phase's first part: every listed ray's cells set
 //                 their bits in the scan's cube bitmap (bxg_mark.cuh).
-//   k_apply_rays  its second half: per marked leaf, get-or-create the leaf and
-//                 apply the miss update to its marked cells.
+//   k_list_touched  the marked leaf blocks onto a list, in cube order.
+//   k_apply_rays  per listed leaf block, get-or-create the leaf and apply the
+//                 miss update to its marked cells.
 //   k_rays        the single-pass form of the ray phase, for scans the cube
 //                 does not cover (rays queued by addHitPoint/addMissPoint,
 //                 kept non-finite points, cubes above the size limit): a group
@@ -240,20 +241,20 @@ __global__ void __launch_bounds__(U == 2 ? 256 : 1024, U == 2 ? 3 : 1) k_rays(co
 // Mark phase: block tasks of consecutive rays of the list (taken from the
 // counter *task, zero at launch), marked by mark_rays_block. Also clears
 // tab[0, tab_n), the scan's endpoint dedup table, for the next scan.
-__global__ void __launch_bounds__(1024) k_mark(const __grid_constant__ DMap M, RayCube Q, const int4* __restrict__ cast,
-                                               uint32_t cast_cap, int ox, int oy, int oz,
+__global__ void __launch_bounds__(1024) k_mark(const __grid_constant__ DMap M, RayCube Q,
+                                               const int4* __restrict__ cast, uint32_t cast_cap,
+                                               int ox, int oy, int oz,
                                                uint4* __restrict__ tab, uint32_t tab_n,
                                                uint32_t* task) {
   __shared__ uint32_t sm[kMarkSmemWords];
-  __shared__ uint32_t s_next, s_task;
+  __shared__ MarkRays<1024> rays;
+  __shared__ uint32_t s_task;
   for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < tab_n; t += gridDim.x * blockDim.x)
     tab[t] = make_uint4(kNone, kNone, kNone, kNone);
   for (int t = threadIdx.x; t < kMarkSmemWords; t += blockDim.x) sm[t] = 0u;
   const uint32_t n_cast = min(ld_volatile(M.ctr + C_CAST), cast_cap);
-  // one task per block (a task ends with a block barrier and the block's
-  // shared-memory flush), at least one four-ray round for every warp
-  const uint32_t min_chunk = (blockDim.x / 32u) * kMarkWarpRays;
-  const uint32_t chunk = max(min_chunk, (n_cast + gridDim.x - 1) / gridDim.x);
+  // one task per block (a task ends with the block's shared-memory flush)
+  const uint32_t chunk = max(1u, (n_cast + gridDim.x - 1) / gridDim.x);
   const uint32_t n_tasks = (n_cast + chunk - 1) / chunk;
   uint32_t visited = 0;
   for (;;) {
@@ -263,14 +264,24 @@ __global__ void __launch_bounds__(1024) k_mark(const __grid_constant__ DMap M, R
     const uint32_t t = s_task;
     if (t >= n_tasks) break;
     const uint32_t r0 = t * chunk;
-    mark_rays_block<kMarkNB>(M, Q, cast, r0, min(n_cast, r0 + chunk), ox, oy, oz, sm, &s_next,
-                             visited);
+    mark_rays_block<kMarkNB, 1024>(M, Q, cast, r0, min(n_cast, r0 + chunk), ox, oy, oz, sm,
+                                   rays, visited);
   }
   visited = __reduce_add_sync(0xffffffffu, visited);
   if ((threadIdx.x & 31) == 0 && visited)
     atomicAdd(reinterpret_cast<unsigned long long*>(M.ctr + C_STATS) + S_VISITED,
               static_cast<unsigned long long>(visited));
 }
+
+// List phase: the marked blocks onto the scan's list (one warp per 32 words
+// of the touched bitmap).
+__global__ void __launch_bounds__(256) k_list_touched(const __grid_constant__ DMap M, RayCube Q) {
+  const uint32_t chunks = (cube_touched_words(Q) + 31u) / 32u;
+  const uint32_t wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t c = wid; c < chunks; c += nw) list_touched(M, Q, c);
+}
+
 
 // Apply phase: a group of kApplyGroup lanes per listed leaf block; D: the
 // map's leaf directory (D.words == nullptr: none).
@@ -506,9 +517,10 @@ int cube_for_scan(bxg_pmap_s* pm, int ox, int oy, int oz, double reach, RayCube*
   const uint32_t S = uint32_t(2 * HL + 1);
   if (S > kMaxCubeSide) return BXG_OK;
   const size_t blocks = size_t(S) * S * S;
+  const uint32_t tmask = cube_touched_mask(S);
   if (blocks > pm->cube_blocks) {
     BXG_CUDA(m, pm->cube_bits.ensure(blocks * 64));
-    BXG_CUDA(m, pm->cube_touch.ensure(((blocks + 31) / 32) * 4));
+    BXG_CUDA(m, pm->cube_touch.ensure((size_t(tmask) + 1) / 8));
     BXG_CUDA(m, pm->cube_list.ensure(blocks * 4));
     BXG_CUDA(m, cudaMemsetAsync(pm->cube_bits.p, 0, pm->cube_bits.cap, m->stream));
     BXG_CUDA(m, cudaMemsetAsync(pm->cube_touch.p, 0, pm->cube_touch.cap, m->stream));
@@ -525,6 +537,7 @@ int cube_for_scan(bxg_pmap_s* pm, int ox, int oy, int oz, double reach, RayCube*
   Q->z0 = ((oz >> 3) - HL) * 8;
   Q->S = S;
   Q->cap = uint32_t(blocks);
+  Q->tmask = tmask;
   *ok = true;
   return BXG_OK;
 }
@@ -564,10 +577,15 @@ int launch_rays(bxg_pmap_s* pm, int ox, int oy, int oz) {
       const uint32_t tab_n = m->dedup_used;
       BXG_CUDA(m, cudaMemsetAsync(m->ctr.as<uint32_t>() + C_LIST, 0, 8, m->stream));
       const unsigned mblocks =
-          unsigned(std::min<uint64_t>(m->sm_count, std::max<uint64_t>(1, pm->cast_ub / 256)));
+          unsigned(std::min<uint64_t>(m->sm_count, std::max<uint64_t>(1, pm->cast_ub / 64)));
       k_mark<<<mblocks, 1024, 0, m->stream>>>(m->dm, Q, m->s_cast.as<int4>(), ccap, ox, oy, oz,
                                              m->s_dedup.as<uint4>(), tab_n,
                                              m->ctr.as<uint32_t>() + C_TASK);
+      BXG_LAUNCHED(m);
+      const uint64_t chunks = (cube_touched_words(Q) + 31u) / 32u;
+      const unsigned lblocks =
+          unsigned(std::min<uint64_t>(uint64_t(m->sm_count) * 8, (chunks + 7) / 8));
+      k_list_touched<<<std::max(lblocks, 1u), 256, 0, m->stream>>>(m->dm, Q);
       BXG_LAUNCHED(m);
       // 256 / kApplyGroup groups per block; the list holds at most
       // min(cube, 64 x rays) blocks
