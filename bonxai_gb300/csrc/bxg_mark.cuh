@@ -422,15 +422,22 @@ __device__ __forceinline__ void apply_block(const DMap& M, const RayCube& Q, uin
   int4* cells = reinterpret_cast<int4*>(reinterpret_cast<int32_t*>(M.ldata) +
                                         static_cast<size_t>(leaf) * 512u + 64u * sl);
   unsigned long long fresh = 0;  // cells whose word was zero: turn their mask bits on
+  // Per bitmap word, the marked 16-byte runs are all loaded before any is
+  // stored: interleaved, each store kept the next load from issuing (the
+  // compiler cannot tell the runs apart), one round trip per run.
 #pragma unroll
   for (int h = 0; h < 2; ++h) {
     const uint32_t w = h ? wv.y : wv.x;
+    if (!w) continue;
+    int4 v[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
+      if ((w >> (4 * j)) & 0xFu) v[j] = cells[8 * h + j];
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
       const uint32_t nib = (w >> (4 * j)) & 0xFu;
       if (!nib) continue;
-      int4 v = cells[8 * h + j];
-      int32_t* c = reinterpret_cast<int32_t*>(&v);
+      int32_t* c = reinterpret_cast<int32_t*>(&v[j]);
       bool changed = false;
 #pragma unroll
       for (int t = 0; t < 4; ++t) {
@@ -443,7 +450,7 @@ __device__ __forceinline__ void apply_block(const DMap& M, const RayCube& Q, uin
         }
         if (old == 0) fresh |= 1ull << (32 * h + 4 * j + t);
       }
-      if (changed) cells[8 * h + j] = v;
+      if (changed) cells[8 * h + j] = v[j];
     }
   }
   if (fresh) red_or64(M.lmask + static_cast<size_t>(leaf) * M.lwords + sl, fresh);
